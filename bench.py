@@ -1,0 +1,297 @@
+"""Benchmark: batched LP solve throughput (LPs/s, pivots/s) on one GB300.
+
+Workloads are the synthetic configurations of include/blpg.h (seeded,
+deterministic; they stand in for the Netlib-sized LPs the reference was run
+on).  One step = one solve of the whole workload batch.
+
+  value        LPs/s with A, b, c already resident in HBM (plan replay; each
+               step re-solves from the input data, nothing is cached)
+  e2e          LPs/s through the public C ABI (blpg_solve_batch) from host
+               buffers: host->device copy of A, b, c and device->host copy of
+               status/objective/pivots inside the timed region
+  roofline     algorithmic bytes per pivot  s * (2 (m+1) W + W + 2 (m+1)),
+               W = n + m + 1, s = 8 (FP64) / 4 (FP32), summed over the LPs'
+               pivots, divided by the CUDA-event time of the solve kernels;
+               peak = shared-memory bandwidth measured live on the device.
+               The FP64 tableau is also bound by the FP64 FMA pipe (one FMA
+               per element per pivot): reported beside it.
+  cpu_baseline the CPU oracle (plain-C restatement of the reference method,
+               all host threads) on a bounded sample of the same workload
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload 0..4]
+                  [--precision fp64|fp32] [--impl blpg|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD_NAMES = {
+    0: "kind0: 1,024 LPs m=28 n=32 density 0.6",
+    1: "kind1: 10,000 LPs m in {50,56,74,105}, n~U[m,1.8m], 10% unbounded, 5% zero-b rows",
+    2: "kind2: 2,048 LPs m=205 n=203 density 0.15",
+    3: "kind3 eval: 10,000 perturbed LPs (m=174, n=142, 64 families)",
+    4: "kind4: 200,000 LPs m log-uniform [16,256], n~U[m/2,2m]",
+}
+L2_BYTES = 129 * 1024 * 1024
+
+
+def workload(kind: int, rank: int = 0, world: int = 1):
+    import simplexprojects_gb300 as sp
+    if kind == 3:
+        count, first = 10_000, 40_000  # the evaluation split
+    else:
+        count, first = sp.WORKLOAD_COUNTS[kind], 0
+    per = (count + world - 1) // world
+    lo = first + rank * per
+    n = max(0, min(per, first + count - lo))
+    return sp.generate(kind, n, seed=sp.DEFAULT_SEED, first=lo, share_family_A=True), count
+
+
+def bytes_per_pivot(m, n, s):
+    W = n + m + 1
+    return s * (2.0 * (m + 1) * W + W + 2.0 * (m + 1))
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.out = ""
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append(dict(sm=float(parts[1]), max=float(parts[2]), power=float(parts[3]),
+                                 hw=parts[5], hwt=parts[6], swt=parts[7], pcap=parts[8]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        loaded = [r for r in rows if r["power"] > 250] or rows
+        reasons = set()
+        for r in loaded:
+            for key, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"),
+                              ("swt", "sw_thermal_slowdown"), ("pcap", "sw_power_cap")):
+                if r[key].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in loaded),
+                "sm_max_mhz": max(r["max"] for r in loaded), "reasons": sorted(reasons),
+                "samples": len(loaded)}
+
+
+def cpu_baseline(batch, precision: str, budget_s: float = 12.0):
+    """The CPU oracle on a bounded sample: LPs/s with all host threads."""
+    from oracle import ref  # CPU baseline leg only
+    threads = os.cpu_count() or 1
+    k = min(batch.count, max(threads * 4, 64))
+    t0 = time.perf_counter()
+    ref.solve_batch(batch.subset(range(k)), precision, threads=threads)
+    dt = time.perf_counter() - t0
+    rate = k / dt
+    k2 = int(min(batch.count, max(k, rate * budget_s)))
+    sample = batch.subset(range(k2))
+    t0 = time.perf_counter()
+    r = ref.solve_batch(sample, precision, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": k2 / dt, "unit": "LPs/s", "cores": threads, "kind": "port",
+            "pivots_per_s": float(r.pivots.sum()) / dt,
+            "sample": f"first {k2} LPs of the workload, {precision} oracle, {dt:.1f}s"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    batch, total = workload(args.workload)
+    warm = [cpu_baseline(batch, args.precision, budget_s=2.0) for _ in range(max(1, args.warmup // 3))]
+    vals = [cpu_baseline(batch, args.precision, budget_s=8.0) for _ in range(args.steps)]
+    v = statistics.median(x["value"] for x in vals)
+    cb = dict(vals[-1], value=v)
+    print(json.dumps({
+        "impl": "reference", "metric": "LPs/s", "value": v, "unit": "LPs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "dtype": "f64" if args.precision == "fp64" else "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_NAMES[args.workload], "precision": args.precision,
+                   "lps": total},
+        "cpu_baseline": cb,
+        "e2e": {"value": v, "unit": "LPs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference arm = CPU oracle (plain-C restatement of BLPG-Solver's method); the "
+                "reference's own CUDA/boost/GLPK build cannot be compiled here",
+        "warm_runs": len(warm),
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", type=int, default=1)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--impl", default="blpg", choices=["blpg", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import simplexprojects_gb300 as sp
+    from simplexprojects_gb300 import _native as N
+    import ctypes as C
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    batch, total = workload(args.workload, rank, world)
+    s = 8 if args.precision == "fp64" else 4
+    db = sp.DeviceBatch(batch, args.precision, device=f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        db.run()
+    torch.cuda.synchronize()
+    res = db.result()
+    pivots = res.pivots.astype(np.float64)
+    alg_bytes = float((pivots * bytes_per_pivot(batch.m.astype(np.float64),
+                                                 batch.n.astype(np.float64), s)).sum())
+    flops = float((pivots * 2.0 * (batch.m + 1.0) * (batch.n + batch.m + 1.0)).sum())
+
+    # ---- value: device-resident inputs (larger than L2 for kinds 1-4) ----
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+    with Clocks(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.fill_(float(i))  # L2 flush between iterations
+            ev[i][0].record(stream)
+            db.run()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    times = [a.elapsed_time(b) for a, b in ev]
+    ms = statistics.median(times)
+    if dist is not None:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = total / (ms * 1e-3)
+
+    # ---- e2e: the public C ABI from host buffers ----
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        barrier()
+        t0 = time.perf_counter()
+        r = sp.solve(batch, args.precision)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2e_times.append(dt)
+    e2e_ms = statistics.median(e2e_times) * 1e3
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    assert np.array_equal(r.status, res.status) and np.array_equal(r.objective, res.objective)
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    smem, f64, f32 = C.c_double(), C.c_double(), C.c_double()
+    N.check(N.lib().blpg_measure_peaks(local, C.byref(smem), C.byref(f64), C.byref(f32)),
+            "blpg_measure_peaks")
+    ach = alg_bytes / (ms * 1e-3) / 1e9
+    ach_tf = flops / (ms * 1e-3) / 1e12
+    fp_peak = f64.value if args.precision == "fp64" else f32.value
+    roof = {"bound": "smem", "achieved": ach, "peak": smem.value, "unit": "GB/s",
+            "frac": ach / smem.value, "traffic": None,
+            "peak_source": "measured live (blpg_measure_peaks: shared-memory stream probe)",
+            "fma_pipe": {"achieved": ach_tf, "peak": fp_peak, "unit": "TFLOP/s",
+                         "frac": ach_tf / fp_peak, "pipe": args.precision}}
+    if roof["fma_pipe"]["frac"] > roof["frac"]:
+        roof["bound_by"] = f"{args.precision} FMA pipe"
+    cpu = None if args.no_cpu_baseline else cpu_baseline(batch, args.precision)
+    h2d = int(batch.A.nbytes + batch.b.nbytes + batch.c.nbytes)
+    d2h = int(batch.count * (4 + 8 + 4))
+    launches = db.plan.launches()
+    out = {
+        "metric": "LPs/s", "value": value, "unit": "LPs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak" if world > 1 else "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
+        "data": "synthetic (seeded generator, include/blpg.h)",
+        "config": {"workload": WORKLOAD_NAMES[args.workload], "lps": total,
+                   "precision": args.precision, "parallelism": "replicas" if world > 1 else "1gpu",
+                   "l2": "inputs larger than L2; L2 flushed between iterations",
+                   "classes": db.plan.classes()},
+        "pivots_per_s": float(pivots.sum()) * world / (ms * 1e-3),
+        "status_counts": np.bincount(res.status, minlength=7).tolist(),
+        "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "LPs/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": launches * args.steps,
+        "step_ms_all": times,
+    }
+    print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,217 @@
+/*
+ * blpg.h — C ABI of the GB300 batched LP solver (libblpg.so).
+ *
+ * Solves a batch of independent dense linear programs
+ *
+ *     maximise  c^T x   subject to  A x <= b,  x >= 0
+ *
+ * with the dense-tableau primal simplex method: slack-basis start, Dantzig
+ * pricing (most negative reduced cost) with lowest-index ties, minimum-ratio
+ * test with lowest-basic-variable-index ties, one LP per CTA (or per
+ * thread-block cluster when the tableau does not fit one CTA's shared memory).
+ *
+ * Reference interface replaced (zzambia/simplexprojects, BLPG-Solver):
+ *   class Simplex                       BLPG-Solver/src/simplex.cuh:37-83
+ *     Simplex(N_S, multipleBatch)       BLPG-Solver/src/simplex.cu:387-400
+ *     setConstratint(A, b)              BLPG-Solver/src/simplex.cu:463-550
+ *     ComputeLP(C, number_of_streams)   BLPG-Solver/src/simplex.cu:552-977
+ *     getResultAll / getStatusAll       BLPG-Solver/src/simplex.cu:424-461
+ *   __global__ mykernel(...)            BLPG-Solver/src/simplex.cu:35-385
+ * The C++ mirror of that class over this ABI is include/blpg_simplex.hpp.
+ *
+ * Conventions: plain pointers and sizes only; every entry point returns 0 on
+ * success or a negative BLPG_E* code, and blpg_last_error() gives a message
+ * (thread-local).  Nothing here falls back to the CPU: without a usable
+ * CUDA device the solve entry points return BLPG_ENODEV.
+ */
+#ifndef BLPG_H_
+#define BLPG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BLPG_ABI_VERSION 1
+
+/* Per-LP status: the numeric codes of GLPK's glp_get_status(), which the
+ * reference's oracle wrapper reports (glpk_lp_solver.cpp:259-273).  The
+ * reference kernel itself only ever reports 2 or 6 (simplex.cu:451-461). */
+enum {
+  BLPG_UNDEF = 1,  /* pivot cap reached before a verdict (GLPK: it_lim) */
+  BLPG_FEAS = 2,
+  BLPG_INFEAS = 3,
+  BLPG_NOFEAS = 4, /* phase I proved that no x satisfies A x <= b, x >= 0 */
+  BLPG_OPT = 5,
+  BLPG_UNBND = 6
+};
+
+/* Error codes returned by the entry points. */
+enum {
+  BLPG_OK = 0,
+  BLPG_EINVAL = -1,  /* bad argument (null pointer, m or n out of range ...) */
+  BLPG_ENODEV = -2,  /* no CUDA device, or the device is not sm_103 */
+  BLPG_ECUDA = -3,   /* a CUDA runtime call failed */
+  BLPG_ENOMEM = -4,  /* device or pinned-host allocation failed */
+  BLPG_ETOOBIG = -5, /* a tableau exceeds the largest cluster's shared memory */
+  BLPG_EIO = -6,     /* file could not be read or parsed */
+  BLPG_ESTATE = -7   /* call out of order (e.g. plan used after destroy) */
+};
+
+/* Arithmetic of the tableau. */
+enum {
+  BLPG_FP64 = 0, /* plain FP64 tableau: the drop-in path */
+  BLPG_FP32 = 1  /* FP32 tableau with FP64 refresh of x_B and reduced costs */
+};
+
+/* Largest LP handled: rows and total tableau columns (n + m + 1). */
+#define BLPG_MAX_ROWS 1024
+#define BLPG_MAX_COLS 8192
+
+/* A batch of LPs in host (or, for blpg_plan_execute, device) memory.
+ * LP k has m[k] rows and n[k] structural columns; its A is row-major
+ * m[k] x n[k] at A + off_A[k], b at b + off_b[k], c at c + off_c[k].
+ * Null offset arrays mean "packed": each LP follows the previous one.
+ * The reference's batch mode (one A, b shared by all LPs, one objective
+ * per LP — GPU_Tester.cu:119-127, simplex.cu:463-466) is off_A[k] = 0,
+ * off_b[k] = 0 for every k. */
+typedef struct blpg_batch {
+  int32_t count;
+  const int32_t* m;
+  const int32_t* n;
+  const int64_t* off_A; /* nullable */
+  const int64_t* off_b; /* nullable */
+  const int64_t* off_c; /* nullable */
+  const double* A;
+  const double* b;
+  const double* c;
+} blpg_batch;
+
+typedef struct blpg_options {
+  int32_t precision;       /* BLPG_FP64 (default) or BLPG_FP32 */
+  int32_t max_pivots;      /* per-LP pivot cap; 0 = 50 * (m + n) + 1000 */
+  int32_t bland_after;     /* consecutive degenerate pivots before Bland's
+                              rule takes over for the rest of the LP; 0 = 64 */
+  int32_t refactor_period; /* FP32 only: FP64 refresh of x_B and reduced costs
+                              every k pivots; 0 = at termination only */
+  double opt_tol;          /* reduced-cost tolerance; 0 = 1e-9 (FP64) / 1e-5 */
+  double piv_tol;          /* pivot tolerance;       0 = 1e-9 (FP64) / 1e-6 */
+  const int32_t* basis_hint; /* nullable warm start: per LP, m[k] column ids
+                                (0..n-1 structural, n..n+m-1 slack), packed
+                                in LP order; see blpg_solve_batch */
+  int32_t device;          /* CUDA device ordinal; default 0 */
+  int32_t use_graph;       /* 1 (default): replay plan launches as a CUDA graph */
+  int32_t threads_per_cta; /* 0 = autotuned per size class */
+  int32_t max_cluster;     /* largest cluster (CTAs per LP) allowed; 0 = 8 */
+  int32_t min_cluster;     /* smallest cluster used even when one CTA would
+                              do (tests of the cluster path); 0 = 1 */
+} blpg_options;
+
+/* Per-LP outputs (host memory for blpg_solve_batch, device memory for
+ * blpg_plan_execute).  status and objective are required; the others may be
+ * null.  x uses the off_c layout of the batch (n[k] values for LP k) when
+ * off_c is given, else packed; basis is packed, m[k] ids per LP. */
+typedef struct blpg_result {
+  int32_t* status;
+  double* objective; /* c^T x of the max problem, as the reference's Result[] */
+  double* x;         /* nullable */
+  int32_t* pivots;   /* nullable: simplex pivots performed per LP */
+  int32_t* basis;    /* nullable: final basic column id of each row */
+} blpg_result;
+
+/* Fill *opt with the defaults above. */
+void blpg_options_init(blpg_options* opt);
+
+/* Solve a host-resident batch; synchronous.  Replaces Simplex::ComputeLP +
+ * getResultAll + getStatusAll (simplex.cu:552-977, :424-461): uploads the
+ * batch, solves every LP on the GPU and downloads the results.  Every b must
+ * be >= 0 except where the LP is solved by the two-phase path (b_i < 0
+ * anywhere in an LP switches that LP to phase I; simplex.cu:574-583). */
+int32_t blpg_solve_batch(const blpg_batch* batch, const blpg_options* opt,
+                         blpg_result* out);
+
+/* Plans: the size classes, work queues, device scratch and CUDA graph for
+ * one batch shape, built once and replayed.  blpg_plan_create reads only the
+ * shapes (count, m, n, offsets) of a HOST batch; A, b, c may be null. */
+typedef struct blpg_plan blpg_plan;
+
+int32_t blpg_plan_create(const blpg_batch* host_shapes, const blpg_options* opt,
+                         blpg_plan** plan);
+
+/* Run a plan on DEVICE-resident data (A, b, c device pointers with the
+ * offsets given at plan creation) into DEVICE-resident outputs, enqueued on
+ * `stream` (a cudaStream_t; null = the legacy default stream).  Asynchronous:
+ * synchronise the stream before reading the outputs.  `basis_hint` (device,
+ * nullable) overrides opt->basis_hint for this run. */
+int32_t blpg_plan_execute(blpg_plan* plan, const double* dA, const double* db,
+                          const double* dc, const int32_t* basis_hint,
+                          blpg_result* dev_out, void* stream);
+
+/* Number of size classes and, per class, CTAs per LP (cluster size),
+ * threads per CTA, dynamic shared memory per CTA and LPs in the class. */
+int32_t blpg_plan_num_classes(const blpg_plan* plan);
+int32_t blpg_plan_class_info(const blpg_plan* plan, int32_t cls,
+                             int32_t* cluster, int32_t* threads,
+                             int32_t* smem_bytes, int32_t* num_lps);
+/* Kernel launches one blpg_plan_execute performs. */
+int32_t blpg_plan_launches(const blpg_plan* plan);
+void blpg_plan_destroy(blpg_plan* plan);
+
+/* Size-class table (JSON text, as written by the autotuner): overrides the
+ * built-in heuristic for threads per CTA and cluster size.  Null resets. */
+int32_t blpg_set_tuning(const char* json_text);
+
+const char* blpg_last_error(void);
+const char* blpg_version(void);
+
+/* Roofline denominators of the pivot kernels, timed on `device` by synthetic
+ * kernels: shared-memory bandwidth (GB/s, bytes read + written) and FP64 /
+ * FP32 FMA throughput (TFLOP/s, 2 flops per FMA).  No reference counterpart
+ * (the reference publishes no performance figures). */
+int32_t blpg_measure_peaks(int32_t device, double* smem_gbs, double* fp64_tflops,
+                           double* fp32_tflops);
+
+/* ---------------------------------------------------------------------------
+ * Reference batch files and synthetic workloads (host only, no GPU needed).
+ * ------------------------------------------------------------------------- */
+
+/* Read the reference's dense A/B/C text files (parseBenchmark.cpp:59-126):
+ * A file: first line "m n", then m lines of n numbers; B: m lines; C: n lines.
+ * Call once with null A, b, c to get *m and *n, then with buffers of
+ * m*n, m and n doubles.  No sign change is applied here: the reference's
+ * driver negates c to turn its minimisation files into max form
+ * (GPU_Tester.cu:119-127); callers do the same. */
+int32_t blpg_read_abc(const char* path_A, const char* path_B,
+                      const char* path_C, int32_t* m, int32_t* n, double* A,
+                      double* b, double* c);
+
+/* Synthetic workloads.  kind 0..4:
+ *  0  m=28, n=32, density 0.6
+ *  1  m in {50,56,74,105}, n uniform on [m, 1.8m], density 0.6,
+ *     10% unbounded LPs, 5% of rows with b_i = 0
+ *  2  m=205, n=203, density 0.15
+ *  3  64 base LPs (m=174, n=142, density 0.2), instance k perturbs base
+ *     k % 64: c_j *= 1 + N(0, 0.1) (clipped > 0), b_i *= U[0.8, 1.2]
+ *  4  m log-uniform on [16, 256], n uniform on [m/2, 2m], density
+ *     U[0.1, 0.6]; 5% unbounded, 5% with degenerate rows, 30% from the
+ *     kind-3 families
+ * A_ij = U[0,1] kept with probability `density`, b_i ~ U[1,10], c_j ~ U[1,5];
+ * LP k draws from its own counter stream seeded with seed + k, so any subset
+ * of a batch can be regenerated alone (first = index of the first LP).
+ * blpg_gen_shapes fills m[count], n[count] (and family[count] if non-null:
+ * the base LP of kind-3 instances, -1 otherwise) and returns the total
+ * number of A elements; blpg_gen_fill writes packed A, b, c. */
+int64_t blpg_gen_shapes(int32_t kind, int64_t first, int32_t count,
+                        uint64_t seed, int32_t* m, int32_t* n,
+                        int32_t* family);
+int32_t blpg_gen_fill(int32_t kind, int64_t first, int32_t count,
+                      uint64_t seed, const int32_t* m, const int32_t* n,
+                      double* A, double* b, double* c, int32_t threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BLPG_H_ */

@@ -1,0 +1,44 @@
+/*
+ * cpu_ref.h — CPU oracle (test infrastructure only; see cpu_ref.c).
+ */
+#ifndef OREF_CPU_REF_H_
+#define OREF_CPU_REF_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* GLPK status codes, as blpg.h. */
+enum { OREF_UNDEF = 1, OREF_NOFEAS = 4, OREF_OPT = 5, OREF_UNBND = 6 };
+enum { OREF_FP64 = 0, OREF_FP32 = 1 };
+
+typedef struct {
+  int precision;
+  int max_pivots;  /* <= 0: 50 (m + n) + 1000 */
+  int bland_after; /* consecutive degenerate pivots before Bland's rule */
+  int refactor_period;
+  double opt_tol, piv_tol, phase1_tol;
+} oref_opts;
+
+void oref_opts_init(oref_opts* o, int precision);
+int oref_default_max_pivots(int m, int n);
+
+int oref_solve_one(int m, int n, const double* A, const double* b,
+                   const double* c, const oref_opts* o, double* obj, double* x,
+                   int* basis, int* pivots);
+
+/* Null offsets = packed.  x (nullable) follows off_c; basis (nullable) is
+ * packed m per LP.  threads = POSIX threads across LPs. */
+int oref_solve_batch(int count, const int* m, const int* n, const int64_t* offA,
+                     const int64_t* offb, const int64_t* offc, const double* A,
+                     const double* b, const double* c, const oref_opts* o,
+                     int threads, int* status, double* obj, double* x,
+                     int* pivots, int* basis);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,21 @@
+"""simplexprojects_gb300 — batched dense-tableau LP solver for one GB300 GPU.
+
+Public API:
+    generate(kind, count, seed)     synthetic workloads 0..4 (include/blpg.h)
+    read_abc(A, B, C)               the reference's dense text files
+    solve(batch, precision)         blocking host-buffer solve (C ABI)
+    Plan, DeviceBatch               plans on device-resident data
+    Simplex                         mirror of the reference's host class
+"""
+from . import _native
+from .lp import LPBatch, generate, read_abc, WORKLOAD_COUNTS, DEFAULT_SEED
+from .solver import DeviceBatch, Plan, Simplex, SolveResult, options, solve
+
+__all__ = [
+    "LPBatch", "generate", "read_abc", "solve", "Plan", "DeviceBatch", "Simplex", "SolveResult",
+    "options", "WORKLOAD_COUNTS", "DEFAULT_SEED",
+]
+
+
+def version() -> str:
+    return _native.lib().blpg_version().decode()

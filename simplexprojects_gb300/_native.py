@@ -1,0 +1,112 @@
+"""ctypes binding of libblpg.so (the C ABI declared in include/blpg.h).
+
+The library is built in-tree by ``simplexprojects_gb300.build`` into
+``simplexprojects_gb300/lib/libblpg.so``.  Loading fails loudly when it is
+missing: there is no Python or CPU fallback for any solve entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libblpg.so"
+
+BLPG_UNDEF, BLPG_FEAS, BLPG_INFEAS, BLPG_NOFEAS, BLPG_OPT, BLPG_UNBND = 1, 2, 3, 4, 5, 6
+BLPG_FP64, BLPG_FP32 = 0, 1
+ERRORS = {
+    -1: "BLPG_EINVAL", -2: "BLPG_ENODEV", -3: "BLPG_ECUDA", -4: "BLPG_ENOMEM",
+    -5: "BLPG_ETOOBIG", -6: "BLPG_EIO", -7: "BLPG_ESTATE",
+}
+
+i32p = C.POINTER(C.c_int32)
+i64p = C.POINTER(C.c_int64)
+f64p = C.POINTER(C.c_double)
+
+
+class Batch(C.Structure):
+    _fields_ = [
+        ("count", C.c_int32), ("m", i32p), ("n", i32p),
+        ("off_A", i64p), ("off_b", i64p), ("off_c", i64p),
+        ("A", f64p), ("b", f64p), ("c", f64p),
+    ]
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int32), ("max_pivots", C.c_int32), ("bland_after", C.c_int32),
+        ("refactor_period", C.c_int32), ("opt_tol", C.c_double), ("piv_tol", C.c_double),
+        ("basis_hint", i32p), ("device", C.c_int32), ("use_graph", C.c_int32),
+        ("threads_per_cta", C.c_int32), ("max_cluster", C.c_int32), ("min_cluster", C.c_int32),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("status", i32p), ("objective", f64p), ("x", f64p), ("pivots", i32p), ("basis", i32p),
+    ]
+
+
+# Every exported symbol of include/blpg.h with its signature.
+SIGNATURES = {
+    "blpg_options_init": (None, [C.POINTER(Options)]),
+    "blpg_solve_batch": (C.c_int32, [C.POINTER(Batch), C.POINTER(Options), C.POINTER(Result)]),
+    "blpg_plan_create": (C.c_int32, [C.POINTER(Batch), C.POINTER(Options), C.POINTER(C.c_void_p)]),
+    "blpg_plan_execute": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.POINTER(Result), C.c_void_p]),
+    "blpg_plan_num_classes": (C.c_int32, [C.c_void_p]),
+    "blpg_plan_class_info": (C.c_int32, [C.c_void_p, C.c_int32, i32p, i32p, i32p, i32p]),
+    "blpg_plan_launches": (C.c_int32, [C.c_void_p]),
+    "blpg_plan_destroy": (None, [C.c_void_p]),
+    "blpg_set_tuning": (C.c_int32, [C.c_char_p]),
+    "blpg_last_error": (C.c_char_p, []),
+    "blpg_version": (C.c_char_p, []),
+    "blpg_measure_peaks": (C.c_int32, [C.c_int32, f64p, f64p, f64p]),
+    "blpg_read_abc": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, i32p, i32p, f64p, f64p, f64p]),
+    "blpg_gen_shapes": (C.c_int64, [C.c_int32, C.c_int64, C.c_int32, C.c_uint64, i32p, i32p, i32p]),
+    "blpg_gen_fill": (C.c_int32, [C.c_int32, C.c_int64, C.c_int32, C.c_uint64, i32p, i32p, f64p,
+                                  f64p, f64p, C.c_int32]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class BlpgError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        msg = lib().blpg_last_error().decode(errors="replace")
+        super().__init__(f"{where}: {ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib() -> C.CDLL:
+    """Load libblpg.so once; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise RuntimeError(
+                    f"{LIB_PATH} is missing: build it with "
+                    "`python -c 'import __graft_entry__ as g; g.build()'` "
+                    "(no CPU fallback exists)")
+            L = C.CDLL(str(LIB_PATH))
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def check(rc: int, where: str) -> None:
+    if rc != 0:
+        raise BlpgError(rc, where)
+
+
+def ptr(a, ctype):
+    """ctypes pointer to a numpy array's data (None for None)."""
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(ctype))

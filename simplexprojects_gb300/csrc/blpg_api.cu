@@ -1,0 +1,714 @@
+// Host side of libblpg.so: plans (size classes + device work queues + CUDA
+// graph), the C ABI entry points and the synchronous host-buffer solve.
+//
+// Reference host path: Simplex::ComputeLP (BLPG-Solver/src/simplex.cu:552-977)
+// builds every tableau on the host with OpenMP, copies the whole tableau
+// batch to the device on N user streams, launches one block per LP with
+// blockDim = 32*(N/32)+32 and copies one objective per LP back, allocating
+// and freeing device memory on every call.  Here the host only uploads
+// A, b, c (tableaux are built in shared memory by the kernel), LPs are
+// grouped into size classes that fix CTAs per LP, threads and shared memory,
+// every class runs as one persistent launch fed by a device ticket queue, and
+// a plan's launches are captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "blpg_internal.h"
+#include "blpg_solver.cuh"
+
+namespace blpg {
+
+static thread_local std::string g_err;
+
+int32_t fail(int32_t code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                  \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess)                                                        \
+      return fail(e_ == cudaErrorMemoryAllocation ? BLPG_ENOMEM : BLPG_ECUDA,     \
+                  "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                                      \
+  } while (0)
+
+using dev::ClassArgs;
+using dev::Geom;
+using dev::Layout;
+using dev::LpArgs;
+
+// Tuning overrides (autotuner JSON): per (precision, K) a threads-per-CTA.
+struct Tuning {
+  std::mutex mu;
+  std::map<std::pair<int, int>, int> threads;  // (precision*16 + K, size bucket)
+};
+static Tuning g_tuning;
+
+static int device_check(int device, cudaDeviceProp* prop) {
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(BLPG_ENODEV, "no CUDA device (%s)", cudaGetErrorString(e));
+  if (device < 0 || device >= ndev)
+    return fail(BLPG_ENODEV, "device %d out of range (%d devices)", device, ndev);
+  CK(cudaGetDeviceProperties(prop, device));
+  if (prop->major != 10 || prop->minor != 3)
+    return fail(BLPG_ENODEV, "device %d is sm_%d%d; libblpg is built for sm_103a only",
+                device, prop->major, prop->minor);
+  return BLPG_OK;
+}
+
+struct ClassPlan {
+  int K = 1, nt = 128, max_m = 0, max_ldw = 0, max_na = 0, smem = 0;
+  int count = 0, grid = 0, order_off = 0;
+  double work = 0;
+};
+
+}  // namespace blpg
+
+struct blpg_plan {
+  int device = 0;
+  blpg_options opt{};
+  int count = 0;
+  int precision = BLPG_FP64;
+  std::vector<int32_t> m, n, na;
+  std::vector<int64_t> offA, offb, offc, offx, offbasis;
+  int64_t extA = 0, extb = 0, extc = 0, extx = 0, extbasis = 0;
+  std::vector<blpg::ClassPlan> classes;
+  std::vector<int32_t> order;
+  // device arrays
+  int32_t *d_m = nullptr, *d_n = nullptr, *d_order = nullptr, *d_tickets = nullptr;
+  int64_t *d_off = nullptr;  // offA | offb | offc | offx | offbasis
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  blpg::LpArgs graph_args{};
+  int launches = 0;
+  int sm_count = 0;
+};
+
+namespace blpg {
+
+static void release(blpg_plan* p) {
+  if (!p) return;
+  if (p->gexec) cudaGraphExecDestroy(p->gexec);
+  cudaFree(p->d_m);
+  cudaFree(p->d_n);
+  cudaFree(p->d_order);
+  cudaFree(p->d_tickets);
+  cudaFree(p->d_off);
+  if (p->ev_in) cudaEventDestroy(p->ev_in);
+  if (p->ev_out) cudaEventDestroy(p->ev_out);
+  if (p->stream) cudaStreamDestroy(p->stream);
+}
+
+template <typename T, bool CL>
+static int set_kernel_attrs(int max_smem) {
+  static std::once_flag once[2];
+  static int rc = 0;
+  (void)once;
+  cudaError_t e = cudaFuncSetAttribute(dev::solve_kernel<T, CL>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+  if (e != cudaSuccess)
+    return fail(BLPG_ECUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+  if (CL) {
+    e = cudaFuncSetAttribute(dev::solve_kernel<T, CL>,
+                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess)
+      return fail(BLPG_ECUDA, "cluster attribute: %s", cudaGetErrorString(e));
+  }
+  return rc;
+}
+
+template <typename T>
+static int occupancy(const ClassPlan& c, int* ctas_per_sm, int* clusters) {
+  *ctas_per_sm = 0;
+  *clusters = 0;
+  if (c.K == 1) {
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm,
+                                                     dev::solve_kernel<T, false>, c.nt,
+                                                     c.smem));
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = c.K;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(c.K, 1, 1);
+    cfg.blockDim = dim3(c.nt, 1, 1);
+    cfg.dynamicSmemBytes = c.smem;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    CK(cudaOccupancyMaxActiveClusters(clusters, dev::solve_kernel<T, true>, &cfg));
+  }
+  return BLPG_OK;
+}
+
+constexpr int kMaxThreads = 512;  // __launch_bounds__ of solve_kernel
+
+// Threads per CTA: whole vector lanes per row group, at least `floor_threads`
+// in total (several row groups for narrow tableaux), at most 1024.
+static int pick_threads(const Geom& g, int precision, int K, int override_nt) {
+  if (override_nt > 0) {
+    int nt = dev::round_up(std::max(override_nt, g.nl), 32);
+    return std::min(nt, kMaxThreads);
+  }
+  int floor_threads = precision == BLPG_FP64 ? 256 : 512;
+  {
+    std::lock_guard<std::mutex> lk(g_tuning.mu);
+    auto it = g_tuning.threads.find({precision * 16 + K, 0});
+    if (it != g_tuning.threads.end()) floor_threads = it->second;
+  }
+  int G = std::max(1, floor_threads / g.nl);
+  int nt = dev::round_up(G * g.nl, 32);
+  if (nt > kMaxThreads) nt = dev::round_up(g.nl, 32);
+  return std::min(nt, kMaxThreads);
+}
+
+template <typename T>
+static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
+  constexpr int V = dev::VecT<T>::V;
+  const int elem = (int)sizeof(T);
+  struct Item {
+    int lp, K, nt, smem, ldw;
+    double work;
+  };
+  std::vector<Item> items(p->count);
+  for (int k = 0; k < p->count; ++k) {
+    const int m = p->m[k], n = p->n[k], na = p->na[k];
+    int chosen = 0;
+    const int min_cluster = std::max(1, std::min(p->opt.min_cluster, max_cluster));
+    for (int K = min_cluster; K <= max_cluster; K *= 2) {
+      Geom g(m, n, na, K, V);
+      Layout L(m, g.ldw, elem);
+      if (L.total <= max_smem && g.nl <= kMaxThreads) {
+        chosen = K;
+        items[k] = {k, K, pick_threads(g, p->precision, K, p->opt.threads_per_cta),
+                    L.total, g.ldw,
+                    (double)(m + 1) * (double)(n + m + 1) * (double)(m + n)};
+        break;
+      }
+    }
+    if (!chosen)
+      return fail(BLPG_ETOOBIG,
+                  "LP %d (m=%d, n=%d) needs more than %d CTAs of shared memory", k, m,
+                  n, max_cluster);
+  }
+  // Group by (K, nt, occupancy level): the class is sized for its largest
+  // member, which keeps the member's own occupancy.
+  std::map<std::tuple<int, int, int>, std::vector<int>> groups;
+  for (auto& it : items) {
+    int per_sm = std::max(1, (228 * 1024) / (it.smem + 1024));
+    per_sm = std::min(per_sm, 2048 / it.nt);
+    groups[{it.K, it.nt, per_sm}].push_back(it.lp);
+  }
+  p->classes.clear();
+  p->order.clear();
+  for (auto& kv : groups) {
+    const int K = std::get<0>(kv.first), nt = std::get<1>(kv.first);
+    const int per_sm_key = std::get<2>(kv.first);
+    // smem budget of the bucket: keep the members' occupancy level
+    const int bucket_smem = std::min(max_smem, (228 * 1024) / per_sm_key - 1024);
+    auto& lps = kv.second;
+    std::stable_sort(lps.begin(), lps.end(),
+                     [&](int a, int b) { return items[a].work > items[b].work; });
+    // Greedy split: a class's layout is sized by its largest m and largest
+    // ldw, which may come from different members; start a new class when
+    // the combined layout would not fit.
+    std::vector<ClassPlan> parts;
+    std::vector<std::vector<int>> members;
+    for (int lp : lps) {
+      bool placed = false;
+      for (size_t ci = 0; ci < parts.size() && !placed; ++ci) {
+        ClassPlan& c = parts[ci];
+        const int mm = std::max(c.max_m, p->m[lp]);
+        const int ll = std::max(c.max_ldw, items[lp].ldw);
+        if (Layout(mm, ll, elem).total <= std::max(bucket_smem, items[lp].smem) &&
+            Layout(mm, ll, elem).total <= max_smem) {
+          c.max_m = mm;
+          c.max_ldw = ll;
+          c.max_na = std::max(c.max_na, p->na[lp]);
+          c.work += items[lp].work;
+          members[ci].push_back(lp);
+          placed = true;
+        }
+      }
+      if (!placed) {
+        ClassPlan c;
+        c.K = K;
+        c.nt = nt;
+        c.max_m = p->m[lp];
+        c.max_ldw = items[lp].ldw;
+        c.max_na = p->na[lp];
+        c.work = items[lp].work;
+        parts.push_back(c);
+        members.push_back({lp});
+      }
+    }
+    for (size_t ci = 0; ci < parts.size(); ++ci) {
+      ClassPlan c = parts[ci];
+      c.smem = Layout(c.max_m, c.max_ldw, elem).total;
+      c.count = (int)members[ci].size();
+      c.order_off = (int)p->order.size();
+      p->order.insert(p->order.end(), members[ci].begin(), members[ci].end());
+      int per_sm = 0, clusters = 0;
+      int rc = occupancy<T>(c, &per_sm, &clusters);
+      if (rc) return rc;
+      int slots = c.K == 1 ? per_sm * p->sm_count : clusters;
+      if (slots <= 0)
+        return fail(BLPG_ETOOBIG, "class K=%d nt=%d smem=%d cannot be resident", c.K,
+                    c.nt, c.smem);
+      c.grid = std::min(slots, c.count) * c.K;
+      p->classes.push_back(c);
+    }
+  }
+  // heaviest class first
+  std::stable_sort(p->classes.begin(), p->classes.end(),
+                   [](const ClassPlan& a, const ClassPlan& b) { return a.work > b.work; });
+  return BLPG_OK;
+}
+
+template <typename T>
+static int launch_classes(blpg_plan* p, const LpArgs& args, cudaStream_t s) {
+  CK(cudaMemsetAsync(p->d_tickets, 0, sizeof(int32_t) * p->classes.size(), s));
+  for (size_t ci = 0; ci < p->classes.size(); ++ci) {
+    const ClassPlan& c = p->classes[ci];
+    ClassArgs ca;
+    ca.order = p->d_order + c.order_off;
+    ca.count = c.count;
+    ca.ticket = p->d_tickets + ci;
+    ca.K = c.K;
+    ca.max_m = c.max_m;
+    ca.max_ldw = c.max_ldw;
+    ca.max_na = c.max_na;
+    if (c.K == 1) {
+      dev::solve_kernel<T, false><<<c.grid, c.nt, c.smem, s>>>(args, ca);
+      CK(cudaGetLastError());
+    } else {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = c.K;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3(c.grid, 1, 1);
+      cfg.blockDim = dim3(c.nt, 1, 1);
+      cfg.dynamicSmemBytes = c.smem;
+      cfg.stream = s;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      CK(cudaLaunchKernelEx(&cfg, dev::solve_kernel<T, true>, args, ca));
+    }
+  }
+  return BLPG_OK;
+}
+
+static int launch_all(blpg_plan* p, const LpArgs& args, cudaStream_t s) {
+  return p->precision == BLPG_FP32 ? launch_classes<float>(p, args, s)
+                                   : launch_classes<double>(p, args, s);
+}
+
+static bool same_args(const LpArgs& a, const LpArgs& b) {
+  return std::memcmp(&a, &b, sizeof(LpArgs)) == 0;
+}
+
+}  // namespace blpg
+
+using namespace blpg;
+
+extern "C" void blpg_options_init(blpg_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->precision = BLPG_FP64;
+  o->use_graph = 1;
+  o->max_cluster = 8;
+}
+
+extern "C" const char* blpg_last_error(void) { return g_err.c_str(); }
+
+extern "C" const char* blpg_version(void) {
+  return "blpg-gb300 1.0 (sm_103a; abi 1)";
+}
+
+extern "C" int32_t blpg_set_tuning(const char* json) {
+  std::lock_guard<std::mutex> lk(g_tuning.mu);
+  g_tuning.threads.clear();
+  if (!json) return BLPG_OK;
+  // Minimal reader for {"fp64_k1": 256, "fp32_k2": 512, ...}
+  const char* s = json;
+  while ((s = std::strchr(s, '"'))) {
+    const char* e = std::strchr(s + 1, '"');
+    if (!e) break;
+    std::string key(s + 1, e - s - 1);
+    const char* colon = std::strchr(e, ':');
+    if (!colon) break;
+    int val = std::atoi(colon + 1);
+    int prec = -1, K = 0;
+    if (std::sscanf(key.c_str(), "fp64_k%d", &K) == 1) prec = BLPG_FP64;
+    else if (std::sscanf(key.c_str(), "fp32_k%d", &K) == 1) prec = BLPG_FP32;
+    if (prec >= 0 && val > 0 && val <= 1024) g_tuning.threads[{prec * 16 + K, 0}] = val;
+    s = colon + 1;
+  }
+  return BLPG_OK;
+}
+
+extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* opt_in,
+                                    blpg_plan** out) {
+  if (!bt || !out || bt->count < 0 || (bt->count > 0 && (!bt->m || !bt->n)))
+    return fail(BLPG_EINVAL, "blpg_plan_create: null batch, shapes or output");
+  *out = nullptr;
+  blpg_options opt;
+  if (opt_in)
+    opt = *opt_in;
+  else
+    blpg_options_init(&opt);
+  if (opt.precision != BLPG_FP64 && opt.precision != BLPG_FP32)
+    return fail(BLPG_EINVAL, "unknown precision %d", opt.precision);
+  if (opt.max_cluster <= 0) opt.max_cluster = 8;
+  if (opt.max_cluster > 8) opt.max_cluster = 8;
+  cudaDeviceProp prop;
+  int rc = device_check(opt.device, &prop);
+  if (rc) return rc;
+  CK(cudaSetDevice(opt.device));
+  std::unique_ptr<blpg_plan> p(new blpg_plan);
+  p->device = opt.device;
+  p->opt = opt;
+  p->precision = opt.precision;
+  p->count = bt->count;
+  p->sm_count = prop.multiProcessorCount;
+  const int N = bt->count;
+  p->m.assign(bt->m, bt->m + N);
+  p->n.assign(bt->n, bt->n + N);
+  p->na.assign(N, 0);
+  p->offA.resize(N);
+  p->offb.resize(N);
+  p->offc.resize(N);
+  p->offx.resize(N);
+  p->offbasis.resize(N);
+  int64_t pa = 0, pb = 0, pc = 0, pbs = 0;
+  for (int k = 0; k < N; ++k) {
+    const int m = p->m[k], n = p->n[k];
+    if (m < 1 || n < 1 || m > BLPG_MAX_ROWS || n + m + 1 > BLPG_MAX_COLS)
+      return fail(BLPG_EINVAL, "LP %d: m=%d n=%d out of range", k, m, n);
+    p->offA[k] = bt->off_A ? bt->off_A[k] : pa;
+    p->offb[k] = bt->off_b ? bt->off_b[k] : pb;
+    p->offc[k] = bt->off_c ? bt->off_c[k] : pc;
+    p->offx[k] = p->offc[k];
+    p->offbasis[k] = pbs;
+    if (p->offA[k] < 0 || p->offb[k] < 0 || p->offc[k] < 0)
+      return fail(BLPG_EINVAL, "LP %d: negative offset", k);
+    pa += (int64_t)m * n;
+    pb += m;
+    pc += n;
+    pbs += m;
+    p->extA = std::max(p->extA, p->offA[k] + (int64_t)m * n);
+    p->extb = std::max(p->extb, p->offb[k] + m);
+    p->extc = std::max(p->extc, p->offc[k] + n);
+    if (bt->b) {
+      int neg = 0;
+      for (int i = 0; i < m; ++i) neg += bt->b[p->offb[k] + i] < 0.0 ? 1 : 0;
+      p->na[k] = neg;
+    }
+  }
+  p->extx = p->extc;
+  p->extbasis = pbs;
+  const int max_smem = (int)prop.sharedMemPerBlockOptin;
+  if (p->precision == BLPG_FP32) {
+    if ((rc = set_kernel_attrs<float, false>(max_smem))) return rc;
+    if ((rc = set_kernel_attrs<float, true>(max_smem))) return rc;
+    rc = build_classes<float>(p.get(), max_smem, opt.max_cluster);
+  } else {
+    if ((rc = set_kernel_attrs<double, false>(max_smem))) return rc;
+    if ((rc = set_kernel_attrs<double, true>(max_smem))) return rc;
+    rc = build_classes<double>(p.get(), max_smem, opt.max_cluster);
+  }
+  if (rc) return rc;
+  p->launches = (int)p->classes.size();
+  // device copies of shapes, offsets and queues
+  const size_t nc = std::max<size_t>(1, p->classes.size());
+  auto fail_free = [&](int code) {
+    release(p.get());
+    return code;
+  };
+  cudaError_t e;
+#define CKF(call)                                                                    \
+  do {                                                                               \
+    e = (call);                                                                      \
+    if (e != cudaSuccess)                                                            \
+      return fail_free(fail(e == cudaErrorMemoryAllocation ? BLPG_ENOMEM : BLPG_ECUDA, \
+                            "%s: %s", #call, cudaGetErrorString(e)));                \
+  } while (0)
+  CKF(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+  CKF(cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming));
+  CKF(cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming));
+  const size_t Nn = std::max(1, N);
+  CKF(cudaMalloc(&p->d_m, sizeof(int32_t) * Nn));
+  CKF(cudaMalloc(&p->d_n, sizeof(int32_t) * Nn));
+  CKF(cudaMalloc(&p->d_order, sizeof(int32_t) * Nn));
+  CKF(cudaMalloc(&p->d_tickets, sizeof(int32_t) * nc));
+  CKF(cudaMalloc(&p->d_off, sizeof(int64_t) * 5 * Nn));
+  if (N > 0) {
+    std::vector<int64_t> off(5 * (size_t)N);
+    std::copy(p->offA.begin(), p->offA.end(), off.begin());
+    std::copy(p->offb.begin(), p->offb.end(), off.begin() + N);
+    std::copy(p->offc.begin(), p->offc.end(), off.begin() + 2 * N);
+    std::copy(p->offx.begin(), p->offx.end(), off.begin() + 3 * N);
+    std::copy(p->offbasis.begin(), p->offbasis.end(), off.begin() + 4 * N);
+    CKF(cudaMemcpy(p->d_m, p->m.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice));
+    CKF(cudaMemcpy(p->d_n, p->n.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice));
+    CKF(cudaMemcpy(p->d_order, p->order.data(), sizeof(int32_t) * N,
+                   cudaMemcpyHostToDevice));
+    CKF(cudaMemcpy(p->d_off, off.data(), sizeof(int64_t) * 5 * N, cudaMemcpyHostToDevice));
+  }
+#undef CKF
+  *out = p.release();
+  return BLPG_OK;
+}
+
+extern "C" int32_t blpg_plan_execute(blpg_plan* p, const double* dA, const double* db,
+                                     const double* dc, const int32_t* basis_hint,
+                                     blpg_result* out, void* stream_v) {
+  (void)basis_hint;
+  if (!p || !out || !out->status || !out->objective)
+    return fail(BLPG_EINVAL, "blpg_plan_execute: null plan or outputs");
+  if (p->count == 0) return BLPG_OK;
+  if (!dA || !db || !dc) return fail(BLPG_EINVAL, "blpg_plan_execute: null A, b or c");
+  CK(cudaSetDevice(p->device));
+  cudaStream_t user = (cudaStream_t)stream_v;
+  LpArgs a{};
+  a.m = p->d_m;
+  a.n = p->d_n;
+  const int N = p->count;
+  a.offA = p->d_off;
+  a.offb = p->d_off + N;
+  a.offc = p->d_off + 2 * N;
+  a.offx = p->d_off + 3 * N;
+  a.offbasis = p->d_off + 4 * N;
+  a.A = dA;
+  a.b = db;
+  a.c = dc;
+  a.status = out->status;
+  a.obj = out->objective;
+  a.x = out->x;
+  a.pivots = out->pivots;
+  a.basis = out->basis;
+  const bool fp32 = p->precision == BLPG_FP32;
+  a.opt_tol = p->opt.opt_tol > 0 ? p->opt.opt_tol : (fp32 ? 1e-5 : 1e-9);
+  a.piv_tol = p->opt.piv_tol > 0 ? p->opt.piv_tol : (fp32 ? 1e-6 : 1e-9);
+  a.phase1_tol = fp32 ? 1e-4 : 1e-7;
+  a.max_pivots = p->opt.max_pivots;
+  a.bland_after = p->opt.bland_after > 0 ? p->opt.bland_after : 64;
+  CK(cudaEventRecord(p->ev_in, user));
+  CK(cudaStreamWaitEvent(p->stream, p->ev_in, 0));
+  if (p->opt.use_graph) {
+    if (!p->gexec || !same_args(a, p->graph_args)) {
+      if (p->gexec) {
+        cudaGraphExecDestroy(p->gexec);
+        p->gexec = nullptr;
+      }
+      cudaGraph_t graph = nullptr;
+      CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = launch_all(p, a, p->stream);
+      cudaError_t ec = cudaStreamEndCapture(p->stream, &graph);
+      if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+      }
+      if (ec != cudaSuccess)
+        return fail(BLPG_ECUDA, "graph capture: %s", cudaGetErrorString(ec));
+      cudaError_t ei = cudaGraphInstantiate(&p->gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ei != cudaSuccess)
+        return fail(BLPG_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+      p->graph_args = a;
+    }
+    CK(cudaGraphLaunch(p->gexec, p->stream));
+  } else {
+    int rc = launch_all(p, a, p->stream);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(p->ev_out, p->stream));
+  CK(cudaStreamWaitEvent(user, p->ev_out, 0));
+  return BLPG_OK;
+}
+
+extern "C" int32_t blpg_plan_num_classes(const blpg_plan* p) {
+  return p ? (int32_t)p->classes.size() : fail(BLPG_EINVAL, "null plan");
+}
+
+extern "C" int32_t blpg_plan_class_info(const blpg_plan* p, int32_t cls, int32_t* cluster,
+                                        int32_t* threads, int32_t* smem_bytes,
+                                        int32_t* num_lps) {
+  if (!p || cls < 0 || cls >= (int32_t)p->classes.size())
+    return fail(BLPG_EINVAL, "blpg_plan_class_info: bad plan or class");
+  const ClassPlan& c = p->classes[cls];
+  if (cluster) *cluster = c.K;
+  if (threads) *threads = c.nt;
+  if (smem_bytes) *smem_bytes = c.smem;
+  if (num_lps) *num_lps = c.count;
+  return BLPG_OK;
+}
+
+extern "C" int32_t blpg_plan_launches(const blpg_plan* p) {
+  return p ? p->launches : fail(BLPG_EINVAL, "null plan");
+}
+
+extern "C" void blpg_plan_destroy(blpg_plan* p) {
+  if (!p) return;
+  cudaSetDevice(p->device);
+  if (p->stream) cudaStreamSynchronize(p->stream);
+  release(p);
+  delete p;
+}
+
+// ---------------------------------------------------------------------------
+// Synchronous host-buffer solve with a small plan cache and a grow-only
+// device workspace (the reference allocated and freed device memory on every
+// ComputeLP call, simplex.cu:589-596, :895, :958).
+// ---------------------------------------------------------------------------
+namespace blpg {
+struct Workspace {
+  std::mutex mu;
+  int device = -1;
+  void* buf = nullptr;
+  size_t cap = 0;
+  blpg_plan* plan = nullptr;
+  std::vector<int32_t> key_shapes;
+  std::vector<int64_t> key_offs;
+  blpg_options key_opt{};
+};
+static Workspace g_ws;
+
+static bool plan_matches(const Workspace& w, const blpg_batch* bt, const blpg_options& o,
+                         const std::vector<int32_t>& shapes,
+                         const std::vector<int64_t>& offs) {
+  return w.plan && std::memcmp(&w.key_opt, &o, sizeof(o)) == 0 && w.key_shapes == shapes &&
+         w.key_offs == offs && w.plan->count == bt->count;
+}
+}  // namespace blpg
+
+extern "C" int32_t blpg_solve_batch(const blpg_batch* bt, const blpg_options* opt_in,
+                                    blpg_result* out) {
+  if (!bt || !out || !out->status || !out->objective)
+    return fail(BLPG_EINVAL, "blpg_solve_batch: null batch or outputs");
+  if (bt->count < 0) return fail(BLPG_EINVAL, "blpg_solve_batch: negative count");
+  if (bt->count == 0) return BLPG_OK;
+  if (!bt->A || !bt->b || !bt->c || !bt->m || !bt->n)
+    return fail(BLPG_EINVAL, "blpg_solve_batch: null A, b, c, m or n");
+  blpg_options opt;
+  if (opt_in)
+    opt = *opt_in;
+  else
+    blpg_options_init(&opt);
+  const int N = bt->count;
+  // plan cache key: shapes, offsets, negative-b counts, options
+  std::vector<int32_t> shapes(3 * (size_t)N);
+  std::vector<int64_t> offs;
+  int64_t pb = 0;
+  for (int k = 0; k < N; ++k) {
+    shapes[3 * k] = bt->m[k];
+    shapes[3 * k + 1] = bt->n[k];
+    const int64_t ob = bt->off_b ? bt->off_b[k] : pb;
+    int neg = 0;
+    if (bt->m[k] > 0)
+      for (int i = 0; i < bt->m[k]; ++i) neg += bt->b[ob + i] < 0.0 ? 1 : 0;
+    shapes[3 * k + 2] = neg;
+    pb += bt->m[k] > 0 ? bt->m[k] : 0;
+  }
+  if (bt->off_A) offs.insert(offs.end(), bt->off_A, bt->off_A + N);
+  if (bt->off_b) offs.insert(offs.end(), bt->off_b, bt->off_b + N);
+  if (bt->off_c) offs.insert(offs.end(), bt->off_c, bt->off_c + N);
+  offs.push_back(bt->off_A ? 1 : 0);
+  offs.push_back(bt->off_b ? 2 : 0);
+  offs.push_back(bt->off_c ? 4 : 0);
+
+  std::lock_guard<std::mutex> lk(g_ws.mu);
+  int rc;
+  if (!plan_matches(g_ws, bt, opt, shapes, offs)) {
+    if (g_ws.plan) {
+      blpg_plan_destroy(g_ws.plan);
+      g_ws.plan = nullptr;
+    }
+    if ((rc = blpg_plan_create(bt, &opt, &g_ws.plan))) return rc;
+    g_ws.key_shapes = shapes;
+    g_ws.key_offs = offs;
+    g_ws.key_opt = opt;
+  }
+  blpg_plan* p = g_ws.plan;
+  // workspace: A | b | c | status | obj | x | pivots | basis (256-byte aligned)
+  auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  const size_t sA = al(sizeof(double) * p->extA), sb = al(sizeof(double) * p->extb),
+               sc = al(sizeof(double) * p->extc), sst = al(sizeof(int32_t) * N),
+               sob = al(sizeof(double) * N), sx = al(sizeof(double) * p->extx),
+               spv = al(sizeof(int32_t) * N), sbs = al(sizeof(int32_t) * p->extbasis);
+  const size_t need = sA + sb + sc + sst + sob + (out->x ? sx : 0) +
+                      (out->pivots ? spv : 0) + (out->basis ? sbs : 0);
+  if (g_ws.cap < need || g_ws.device != p->device) {
+    if (g_ws.buf) cudaFree(g_ws.buf);
+    g_ws.buf = nullptr;
+    g_ws.cap = 0;
+    CK(cudaMalloc(&g_ws.buf, need));
+    g_ws.cap = need;
+    g_ws.device = p->device;
+  }
+  char* base = (char*)g_ws.buf;
+  double* dA = (double*)base;
+  double* db = (double*)(base + sA);
+  double* dc = (double*)(base + sA + sb);
+  char* o = base + sA + sb + sc;
+  blpg_result dres{};
+  dres.status = (int32_t*)o;
+  o += sst;
+  dres.objective = (double*)o;
+  o += sob;
+  if (out->x) {
+    dres.x = (double*)o;
+    o += sx;
+  }
+  if (out->pivots) {
+    dres.pivots = (int32_t*)o;
+    o += spv;
+  }
+  if (out->basis) {
+    dres.basis = (int32_t*)o;
+    o += sbs;
+  }
+  cudaStream_t s = p->stream;
+  CK(cudaMemcpyAsync(dA, bt->A, sizeof(double) * p->extA, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(db, bt->b, sizeof(double) * p->extb, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dc, bt->c, sizeof(double) * p->extc, cudaMemcpyHostToDevice, s));
+  if ((rc = blpg_plan_execute(p, dA, db, dc, nullptr, &dres, s))) return rc;
+  CK(cudaMemcpyAsync(out->status, dres.status, sizeof(int32_t) * N, cudaMemcpyDeviceToHost,
+                     s));
+  CK(cudaMemcpyAsync(out->objective, dres.objective, sizeof(double) * N,
+                     cudaMemcpyDeviceToHost, s));
+  if (out->x)
+    CK(cudaMemcpyAsync(out->x, dres.x, sizeof(double) * p->extx, cudaMemcpyDeviceToHost, s));
+  if (out->pivots)
+    CK(cudaMemcpyAsync(out->pivots, dres.pivots, sizeof(int32_t) * N,
+                       cudaMemcpyDeviceToHost, s));
+  if (out->basis)
+    CK(cudaMemcpyAsync(out->basis, dres.basis, sizeof(int32_t) * p->extbasis,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  return BLPG_OK;
+}

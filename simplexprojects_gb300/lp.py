@@ -1,0 +1,186 @@
+"""LP batches: the host-side container, the synthetic workloads and the
+reference's A/B/C text files.
+
+A batch holds LP k as ``max c_k^T x  s.t.  A_k x <= b_k, x >= 0`` with A_k
+row-major m_k x n_k.  Offsets let LPs share data: the reference's batch mode
+(one A, b for the whole batch, one objective per LP; GPU_Tester.cu:119-127)
+is ``off_A = off_b = 0`` for every LP, and the perturbed families of workload
+3 share each family's A.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+from . import _native as N
+
+# Workload sizes of the benchmark configurations (kind -> default count).
+WORKLOAD_COUNTS = {0: 1024, 1: 10_000, 2: 2048, 3: 50_000, 4: 200_000}
+DEFAULT_SEED = 20240611
+
+
+@dataclass
+class LPBatch:
+    m: np.ndarray
+    n: np.ndarray
+    A: np.ndarray
+    b: np.ndarray
+    c: np.ndarray
+    off_A: Optional[np.ndarray] = None
+    off_b: Optional[np.ndarray] = None
+    off_c: Optional[np.ndarray] = None
+    family: Optional[np.ndarray] = None
+    meta: dict = field(default_factory=dict)
+
+    def __post_init__(self):
+        self.m = np.ascontiguousarray(self.m, dtype=np.int32)
+        self.n = np.ascontiguousarray(self.n, dtype=np.int32)
+        self.A = np.ascontiguousarray(self.A, dtype=np.float64)
+        self.b = np.ascontiguousarray(self.b, dtype=np.float64)
+        self.c = np.ascontiguousarray(self.c, dtype=np.float64)
+        for name in ("off_A", "off_b", "off_c"):
+            v = getattr(self, name)
+            if v is not None:
+                setattr(self, name, np.ascontiguousarray(v, dtype=np.int64))
+
+    @property
+    def count(self) -> int:
+        return int(self.m.shape[0])
+
+    def offsets(self):
+        """(off_A, off_b, off_c), computing packed offsets where absent."""
+        mn = self.m.astype(np.int64) * self.n
+        pa = np.concatenate([[0], np.cumsum(mn)[:-1]]).astype(np.int64)
+        pb = np.concatenate([[0], np.cumsum(self.m.astype(np.int64))[:-1]]).astype(np.int64)
+        pc = np.concatenate([[0], np.cumsum(self.n.astype(np.int64))[:-1]]).astype(np.int64)
+        return (self.off_A if self.off_A is not None else pa,
+                self.off_b if self.off_b is not None else pb,
+                self.off_c if self.off_c is not None else pc)
+
+    def lp(self, k: int):
+        """(A_k as an m x n array, b_k, c_k) for LP k."""
+        oA, ob, oc = self.offsets()
+        m, n = int(self.m[k]), int(self.n[k])
+        A = self.A[oA[k]:oA[k] + m * n].reshape(m, n)
+        return A, self.b[ob[k]:ob[k] + m], self.c[oc[k]:oc[k] + n]
+
+    def subset(self, idx) -> "LPBatch":
+        """A packed copy of the LPs listed in idx."""
+        idx = np.asarray(idx, dtype=np.int64)
+        As, bs, cs = [], [], []
+        for k in idx:
+            A, b, c = self.lp(int(k))
+            As.append(A.ravel())
+            bs.append(b)
+            cs.append(c)
+        fam = self.family[idx] if self.family is not None else None
+        return LPBatch(self.m[idx], self.n[idx],
+                       np.concatenate(As) if As else np.zeros(0),
+                       np.concatenate(bs) if bs else np.zeros(0),
+                       np.concatenate(cs) if cs else np.zeros(0), family=fam,
+                       meta=dict(self.meta, subset=True))
+
+    def c_struct(self) -> N.Batch:
+        """ctypes view; the arrays must outlive the returned struct."""
+        return N.Batch(self.count, N.ptr(self.m, C.c_int32), N.ptr(self.n, C.c_int32),
+                       N.ptr(self.off_A, C.c_int64), N.ptr(self.off_b, C.c_int64),
+                       N.ptr(self.off_c, C.c_int64), N.ptr(self.A, C.c_double),
+                       N.ptr(self.b, C.c_double), N.ptr(self.c, C.c_double))
+
+    def nbytes(self) -> int:
+        return int(self.A.nbytes + self.b.nbytes + self.c.nbytes)
+
+    @classmethod
+    def from_lps(cls, lps) -> "LPBatch":
+        """Packed batch from a list of (A, b, c)."""
+        ms, ns, As, bs, cs = [], [], [], [], []
+        for A, b, c in lps:
+            A = np.asarray(A, dtype=np.float64)
+            ms.append(A.shape[0])
+            ns.append(A.shape[1])
+            As.append(A.ravel())
+            bs.append(np.asarray(b, dtype=np.float64))
+            cs.append(np.asarray(c, dtype=np.float64))
+        return cls(np.array(ms), np.array(ns), np.concatenate(As), np.concatenate(bs),
+                   np.concatenate(cs))
+
+    @classmethod
+    def shared(cls, A, b, C_rows) -> "LPBatch":
+        """The reference's batch mode: one A, b and one objective per LP
+        (rows of C_rows), as Simplex::setConstratint + ComputeLP(C)."""
+        A = np.asarray(A, dtype=np.float64)
+        C_rows = np.asarray(C_rows, dtype=np.float64)
+        k = C_rows.shape[0]
+        m, n = A.shape
+        return cls(np.full(k, m), np.full(k, n), A.ravel(), np.asarray(b, dtype=np.float64),
+                   C_rows.ravel(), off_A=np.zeros(k, np.int64), off_b=np.zeros(k, np.int64),
+                   off_c=np.arange(k, dtype=np.int64) * n)
+
+
+def generate(kind: int, count: Optional[int] = None, seed: int = DEFAULT_SEED, first: int = 0,
+             threads: int = 0, share_family_A: bool = False) -> LPBatch:
+    """Synthetic workload `kind` (0..4, see include/blpg.h): LPs first ..
+    first+count-1 of the stream seeded with `seed`.  With share_family_A, LPs
+    of the perturbed families (kinds 3 and 4) point at one copy of their
+    family's A (they are identical by construction)."""
+    L = N.lib()
+    if count is None:
+        count = WORKLOAD_COUNTS[kind]
+    m = np.zeros(count, np.int32)
+    n = np.zeros(count, np.int32)
+    fam = np.zeros(count, np.int32)
+    total = L.blpg_gen_shapes(kind, first, count, seed, N.ptr(m, C.c_int32), N.ptr(n, C.c_int32),
+                              N.ptr(fam, C.c_int32))
+    if total < 0:
+        N.check(int(total), "blpg_gen_shapes")
+    A = np.empty(int(total), np.float64)
+    b = np.empty(int(m.sum()), np.float64)
+    c = np.empty(int(n.sum()), np.float64)
+    rc = L.blpg_gen_fill(kind, first, count, seed, N.ptr(m, C.c_int32), N.ptr(n, C.c_int32),
+                         N.ptr(A, C.c_double), N.ptr(b, C.c_double), N.ptr(c, C.c_double), threads)
+    N.check(rc, "blpg_gen_fill")
+    batch = LPBatch(m, n, A, b, c, family=fam,
+                    meta=dict(kind=kind, seed=seed, first=first, count=count))
+    if share_family_A and (fam >= 0).any():
+        batch = _share_family_A(batch)
+    return batch
+
+
+def _share_family_A(batch: LPBatch) -> LPBatch:
+    oA, ob, oc = batch.offsets()
+    fam = batch.family
+    keep = {}
+    pieces = []
+    pos = 0
+    new_oA = np.empty(batch.count, np.int64)
+    for k in range(batch.count):
+        f = int(fam[k])
+        key = ("f", f) if f >= 0 else ("k", k)
+        if key not in keep:
+            size = int(batch.m[k]) * int(batch.n[k])
+            pieces.append(batch.A[oA[k]:oA[k] + size])
+            keep[key] = pos
+            pos += size
+        new_oA[k] = keep[key]
+    return LPBatch(batch.m, batch.n, np.concatenate(pieces), batch.b, batch.c, off_A=new_oA,
+                   off_b=ob, off_c=oc, family=batch.family, meta=dict(batch.meta, shared_A=True))
+
+
+def read_abc(path_A: str, path_B: str, path_C: str):
+    """Read the reference's dense A/B/C text files (parseBenchmark.cpp:59-126).
+    Returns (A, b, c) as written (minimisation files: negate c for max form)."""
+    L = N.lib()
+    m = C.c_int32()
+    n = C.c_int32()
+    N.check(L.blpg_read_abc(path_A.encode(), path_B.encode(), path_C.encode(), C.byref(m),
+                            C.byref(n), None, None, None), "blpg_read_abc")
+    A = np.empty(m.value * n.value)
+    b = np.empty(m.value)
+    c = np.empty(n.value)
+    N.check(L.blpg_read_abc(path_A.encode(), path_B.encode(), path_C.encode(), C.byref(m),
+                            C.byref(n), N.ptr(A, C.c_double), N.ptr(b, C.c_double),
+                            N.ptr(c, C.c_double)), "blpg_read_abc")
+    return A.reshape(m.value, n.value), b, c

@@ -1,0 +1,145 @@
+"""Generate the committed golden fixtures (tests/golden/*.json).
+
+Runs in the x86 container only: it calls GLPK 4.45 from the reference's
+prebuilt lib/libglpk.so.0.30.0 (glp_simplex with default parameters, as the
+reference's glpk_lp_solver.cpp:435-454, and glp_exact over GMP rationals as
+the exact judge).  The LP data itself is not stored: every fixture names the
+workload kind, seed and LP indices, and a SHA-256 of the generated A, b, c so
+that a change of the generator is caught.
+
+Fixtures:
+  workloads.json   per workload kind 0..4, a sample of seeded LPs with GLPK's
+                   status/objective and glp_exact's status/objective
+  known.json       the reference's hand LPs (parseBenchmark.cpp:128-319,
+                   GPU_Tester.cu:80-86) and the 8 Netlib LPs it ships
+                   (benchmarks/*.txt, listed optima parseBenchmark.cpp:15-25),
+                   solved by GLPK and glp_exact
+
+Usage:  python tests/golden/make_golden.py [--quick]
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import multiprocessing as mp
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+SEED = 20240611
+# (kind, first, count): LP indices of each workload's sample
+SAMPLES = {0: (0, 48), 1: (0, 40), 2: (0, 3), 3: (39_990, 6), 4: (0, 40)}
+REF = Path("/root/reference")
+NETLIB = ["ADLITTLE", "AFIRO", "BLEND", "ISRAEL", "SC105", "SC205", "SC50A", "SC50B"]
+# listed optima of the minimisation files (parseBenchmark.cpp:15-25)
+NETLIB_LISTED = {
+    "ADLITTLE": 2.2549496316e05, "AFIRO": -4.6475314286e02, "BLEND": -3.0812149846e01,
+    "ISRAEL": -8.9664482186e05, "SC105": -5.2202061212e01, "SC205": -5.2202061212e01,
+    "SC50A": -6.4575077059e01, "SC50B": -7.0000000000e01,
+}
+
+
+def hand_lps():
+    """The reference's hand-written LPs (max c^T x, A x <= b, x >= 0), with the
+    answers its comments state (None where the comment is wrong or absent)."""
+    lps = {
+        # parseSmallLP, parseBenchmark.cpp:128-148 ("unbounded ... at 2")
+        "SmallLP": ([[2, -1], [1, -5]], [2, -4], [2, -1], None),
+        # parseSmallLP2, :151-173, "has solution 39.44444"
+        "SmallLP2": ([[1, 1], [-1, 1], [5, 4]], [10, -3, 35], [5, 6], 39.44444),
+        # parseSmallLP3, :175-197, "has solution 21.33333"
+        "SmallLP3": ([[1, -1], [-1, -1], [-1, 4]], [8, -3, 2], [1, 3], 21.33333),
+        # parseSmallLP4, :199-221, "has solution 9.33333"
+        "SmallLP4": ([[1, 1, -1], [-3, 1, 0], [1, -2, -2]], [7, -8, 0], [2, 0, -6], 9.33333),
+        # parseSmallLP5, :223-245 (its comment repeats LP2's value)
+        "SmallLP5": ([[4, -1], [2, 1], [-5, 2]], [8, 10, 2], [1, 1], None),
+    }
+    # parse5Dim, :252-277: box 0.99 <= x1 <= 1.01, |x_i| <= 0.01 otherwise
+    A5 = np.zeros((10, 5))
+    for i in range(5):
+        A5[2 * i, i] = 1
+        A5[2 * i + 1, i] = -1
+    b5 = [1.01, -0.99] + [0.01] * 8
+    lps["FiveDim_x1"] = (A5.tolist(), b5, [1, 0, 0, 0, 0], 1.01)
+    lps["FiveDim_x2"] = (A5.tolist(), b5, [0, 1, 0, 0, 0], None)
+    # parse28DimHelicopter, :282-319
+    AH = np.zeros((56, 28))
+    bH = np.zeros(56)
+    for i in range(28):
+        AH[2 * i, i] = 1
+        AH[2 * i + 1, i] = -1
+        if i < 8:
+            bH[2 * i] = 0.1
+    cH = np.zeros(28)
+    cH[0] = 1
+    lps["Helicopter28"] = (AH.tolist(), bH.tolist(), cH.tolist(), None)
+    return lps
+
+
+def fingerprint(batch) -> str:
+    h = hashlib.sha256()
+    for a in (batch.m, batch.n, batch.A, batch.b, batch.c):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def _solve_one(args):
+    A, b, c = args
+    from oracle import glpk
+    r = glpk.solve(np.asarray(A), np.asarray(b), np.asarray(c), exact=True)
+    return {k: r[k] for k in ("status", "objective", "exact_status", "exact_objective")}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--quick", action="store_true", help="smaller samples (smoke the script)")
+    ap.add_argument("--procs", type=int, default=8)
+    args = ap.parse_args()
+    import simplexprojects_gb300 as sp
+    from oracle import glpk
+    if not glpk.available():
+        sys.exit("GLPK library not found (the reference's lib/ is needed)")
+    ctx = mp.get_context("spawn")
+    t0 = time.time()
+    out = {"seed": SEED, "glpk_version": glpk.lib().glp_version().decode(), "workloads": {}}
+    with ctx.Pool(args.procs) as pool:
+        for kind, (first, count) in SAMPLES.items():
+            if args.quick:
+                count = min(count, 4)
+            batch = sp.generate(kind, count, seed=SEED, first=first)
+            jobs = [batch.lp(k) for k in range(count)]
+            res = pool.map(_solve_one, [(A.tolist(), b.tolist(), c.tolist()) for A, b, c in jobs])
+            out["workloads"][str(kind)] = {
+                "first": first, "count": count, "sha256": fingerprint(batch),
+                "m": batch.m.tolist(), "n": batch.n.tolist(), "lps": res,
+            }
+            print(f"kind {kind}: {count} LPs, {time.time() - t0:.0f}s", flush=True)
+        (HERE / "workloads.json").write_text(json.dumps(out, indent=1))
+        known = {"hand": {}, "netlib": {}}
+        for name, (A, b, c, stated) in hand_lps().items():
+            r = _solve_one((A, b, c))
+            known["hand"][name] = dict(r, A=A, b=b, c=c, stated=stated)
+        names = [nm for nm in NETLIB if (REF / "benchmarks" / f"{nm}_A.txt").exists()]
+        jobs = []
+        for nm in names:
+            A, b, c = sp.read_abc(*(str(REF / "benchmarks" / f"{nm}_{s}.txt") for s in "ABC"))
+            jobs.append((A.tolist(), b.tolist(), (-c).tolist()))  # max form (GPU_Tester.cu:119-127)
+        res = pool.map(_solve_one, jobs)
+        for nm, (A, b, c), r in zip(names, jobs, res):
+            Aa = np.asarray(A)
+            known["netlib"][nm] = dict(r, m=Aa.shape[0], n=Aa.shape[1],
+                                       negative_b=int((np.asarray(b) < 0).sum()),
+                                       listed_min=NETLIB_LISTED[nm])
+        (HERE / "known.json").write_text(json.dumps(known, indent=1))
+    print(f"done in {time.time() - t0:.0f}s")
+
+
+if __name__ == "__main__":
+    main()

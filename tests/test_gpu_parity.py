@@ -1,0 +1,177 @@
+"""GPU parity: the CUDA solver against the CPU oracle, through the C ABI.
+
+FP64: the kernels apply the oracle's pivot rules with the same IEEE
+operations (fused eliminations, divided pivot row), so statuses, pivot
+counts, final bases, x and objectives must be BIT-IDENTICAL.
+FP32: statuses and pivot counts identical to the FP32 oracle; objectives
+within 1e-6 relative of the FP64 oracle (the FP32 form's tolerance).
+"""
+import numpy as np
+import pytest
+
+import simplexprojects_gb300 as sp
+from oracle import ref
+
+pytestmark = pytest.mark.gpu
+
+FP32_REL = 1e-6
+
+
+def _rel(a, b):
+    return np.abs(a - b) / np.maximum(np.abs(b), 1.0)
+
+
+def assert_bit_identical(gpu, cpu):
+    assert np.array_equal(gpu.status, cpu.status)
+    assert np.array_equal(gpu.pivots, cpu.pivots)
+    assert np.array_equal(gpu.objective.view(np.uint64), cpu.objective.view(np.uint64))
+    if gpu.basis is not None:
+        assert np.array_equal(gpu.basis, cpu.basis)
+    if gpu.x is not None:
+        assert np.array_equal(gpu.x.view(np.uint64), cpu.x.view(np.uint64))
+
+
+@pytest.mark.parametrize("kind,count", [(0, 512), (1, 512), (2, 16), (3, 64), (4, 384)])
+def test_fp64_bit_identical(built, kind, count):
+    batch = sp.generate(kind, count, seed=sp.DEFAULT_SEED + 17 * kind)
+    gpu = sp.solve(batch, "fp64", want_x=True, want_basis=True)
+    cpu = ref.solve_batch(batch, "fp64", want_x=True, want_basis=True)
+    assert_bit_identical(gpu, cpu)
+
+
+@pytest.mark.parametrize("min_cluster", [2, 4, 8])
+def test_fp64_cluster_split_bit_identical(built, min_cluster):
+    """Tableaux split across 2/4/8 CTAs (DSMEM exchange) give the same bits."""
+    batch = sp.generate(1, 96, seed=99)
+    gpu = sp.solve(batch, "fp64", want_x=True, want_basis=True, min_cluster=min_cluster)
+    cpu = ref.solve_batch(batch, "fp64", want_x=True, want_basis=True)
+    assert_bit_identical(gpu, cpu)
+
+
+@pytest.mark.parametrize("kind,count", [(0, 256), (1, 256), (3, 32), (4, 256)])
+def test_fp32_against_oracle(built, kind, count):
+    batch = sp.generate(kind, count, seed=5 + kind)
+    g32 = sp.solve(batch, "fp32", want_basis=True)
+    c32 = ref.solve_batch(batch, "fp32", want_basis=True)
+    c64 = ref.solve_batch(batch, "fp64")
+    assert np.array_equal(g32.status, c32.status)
+    assert np.array_equal(g32.pivots, c32.pivots)
+    assert np.array_equal(g32.status, c64.status)
+    opt = c64.status == 5
+    assert _rel(g32.objective[opt], c64.objective[opt]).max() <= FP32_REL
+
+
+def test_fp32_cluster_split(built):
+    batch = sp.generate(4, 64, seed=3)
+    a = sp.solve(batch, "fp32")
+    b = sp.solve(batch, "fp32", min_cluster=4)
+    assert np.array_equal(a.status, b.status)
+    assert np.array_equal(a.pivots, b.pivots)
+    assert np.array_equal(a.objective, b.objective)
+
+
+def test_golden_statuses_and_exact_objectives(built, workloads_golden):
+    """GLPK's statuses exactly; objectives within 1e-9 (FP64) / 1e-6 (FP32)
+    of glp_exact's rational optimum."""
+    for kind, w in workloads_golden["workloads"].items():
+        batch = sp.generate(int(kind), w["count"], seed=workloads_golden["seed"], first=w["first"])
+        st = np.array([r["exact_status"] for r in w["lps"]])
+        ex = np.array([r["exact_objective"] for r in w["lps"]])
+        for prec, tol in (("fp64", 1e-9), ("fp32", FP32_REL)):
+            g = sp.solve(batch, prec)
+            assert np.array_equal(g.status, st), (kind, prec)
+            opt = st == 5
+            assert _rel(g.objective[opt], ex[opt]).max() <= tol, (kind, prec)
+
+
+def test_two_phase_known_answers(built, known_golden):
+    """The reference's hand LPs (several need phase I): GLPK's status and
+    objective, and bit-identical to the oracle."""
+    lps = list(known_golden["hand"].items())
+    batch = sp.LPBatch.from_lps([(v["A"], v["b"], v["c"]) for _, v in lps])
+    gpu = sp.solve(batch, "fp64", want_x=True, want_basis=True)
+    cpu = ref.solve_batch(batch, "fp64", want_x=True, want_basis=True)
+    assert_bit_identical(gpu, cpu)
+    for k, (name, v) in enumerate(lps):
+        assert gpu.status[k] == v["exact_status"], name
+        if v["exact_status"] == 5:
+            assert abs(gpu.objective[k] - v["exact_objective"]) <= 1e-9 * max(1, abs(v["exact_objective"])), name
+
+
+def test_reference_batch_mode_shared_A_b(built):
+    """One A, b and one objective per LP (Simplex::setConstratint + ComputeLP)."""
+    base = sp.generate(1, 1, seed=1234)
+    A, b, _ = base.lp(0)
+    rng = np.random.default_rng(0)
+    C = rng.uniform(-1, 5, size=(300, A.shape[1]))
+    s = sp.Simplex(300, 0)
+    s.setConstratint(A, b)
+    s.ComputeLP(C, 10)
+    batch = sp.LPBatch.shared(A, b, C)
+    cpu = ref.solve_batch(batch, "fp64")
+    assert np.array_equal(s.getStatusAll(), cpu.status)
+    assert np.array_equal(s.getResultAll().view(np.uint64), cpu.objective.view(np.uint64))
+    assert s.getResult(3) == cpu.objective[2] and s.getStatus(3) == cpu.status[2]
+
+
+def test_device_plan_graph_replay(built):
+    """Device-resident plan: graph replays give identical results."""
+    import torch
+    batch = sp.generate(1, 256, seed=77)
+    db = sp.DeviceBatch(batch, "fp64", want_x=True, want_basis=True)
+    outs = []
+    for _ in range(3):
+        db.status.zero_()
+        db.objective.zero_()
+        db.run()
+        outs.append(db.result())
+    torch.cuda.synchronize()
+    cpu = ref.solve_batch(batch, "fp64", want_x=True, want_basis=True)
+    for o in outs:
+        assert_bit_identical(o, cpu)
+    assert db.plan.launches() == len(db.plan.classes())
+
+
+def test_edge_cases(built):
+    lps = [
+        (np.array([[1.0]]), np.array([2.0]), np.array([3.0])),          # m = n = 1
+        (np.ones((3, 4)), np.ones(3), np.zeros(4)),                      # c = 0: optimal at start
+        (np.array([[-1.0, 1.0]]), np.array([1.0]), np.array([1.0, 0.0])),  # unbounded
+        (np.array([[1.0, 1.0], [1.0, -1.0]]), np.array([0.0, 0.0]), np.array([1.0, 1.0])),  # degenerate
+        (np.zeros((2, 2)), np.array([1.0, 1.0]), np.array([-1.0, -2.0])),  # all-zero A
+    ]
+    batch = sp.LPBatch.from_lps(lps)
+    gpu = sp.solve(batch, "fp64", want_x=True, want_basis=True)
+    cpu = ref.solve_batch(batch, "fp64", want_x=True, want_basis=True)
+    assert_bit_identical(gpu, cpu)
+    assert gpu.status.tolist() == [5, 5, 6, 5, 5]
+    assert gpu.objective[0] == 6.0 and gpu.pivots[1] == 0 and gpu.objective[3] == 0.0
+
+
+def test_largest_workload_shape(built):
+    """m = 256, n = 512 (the largest kind-4 shape): FP64 needs an 8-CTA cluster."""
+    rng = np.random.default_rng(3)
+    A = rng.uniform(0, 1, (256, 512)) * (rng.uniform(size=(256, 512)) < 0.3)
+    b = rng.uniform(1, 10, 256)
+    c = rng.uniform(1, 5, 512)
+    batch = sp.LPBatch.from_lps([(A, b, c)])
+    plan = sp.Plan(batch, "fp64")
+    assert plan.classes()[0]["cluster"] == 8
+    plan.close()
+    gpu = sp.solve(batch, "fp64", want_x=True, want_basis=True)
+    cpu = ref.solve_batch(batch, "fp64", want_x=True, want_basis=True)
+    assert_bit_identical(gpu, cpu)
+
+
+def test_empty_batch_and_errors(built):
+    empty = sp.LPBatch(np.zeros(0), np.zeros(0), np.zeros(0), np.zeros(0), np.zeros(0))
+    r = sp.solve(empty)
+    assert r.status.size == 0
+    bad = sp.LPBatch(np.array([0]), np.array([2]), np.zeros(0), np.zeros(0), np.zeros(2))
+    with pytest.raises(sp._native.BlpgError) as e:
+        sp.solve(bad)
+    assert e.value.code == -1
+    big = sp.LPBatch.from_lps([(np.ones((900, 900)), np.ones(900), np.ones(900))])
+    with pytest.raises(sp._native.BlpgError) as e:
+        sp.solve(big)
+    assert e.value.code == -5
