@@ -97,7 +97,7 @@ typedef struct blpg_options {
   int32_t refactor_period; /* FP32 only: FP64 refresh of x_B and reduced costs
                               every k pivots; 0 = at termination only */
   double opt_tol;          /* reduced-cost tolerance; 0 = 1e-9 (FP64) / 1e-5 */
-  double piv_tol;          /* pivot tolerance;       0 = 1e-9 (FP64) / 1e-6 */
+  double piv_tol;          /* pivot tolerance;       0 = 1e-7 (FP64) / 1e-5 */
   const int32_t* basis_hint; /* nullable warm start: per LP, m[k] column ids
                                 (0..n-1 structural, n..n+m-1 slack), packed
                                 in LP order; see blpg_solve_batch */
@@ -107,6 +107,14 @@ typedef struct blpg_options {
   int32_t max_cluster;     /* largest cluster (CTAs per LP) allowed; 0 = 8 */
   int32_t min_cluster;     /* smallest cluster used even when one CTA would
                               do (tests of the cluster path); 0 = 1 */
+  int32_t cta_smem_budget; /* shared memory per CTA that picks each LP's
+                              cluster size; 0 = autotuned (default: half an
+                              SM, i.e. two CTAs per SM) */
+  int32_t ratio_rule;      /* 0 (default): Harris two-pass ratio test (largest
+                              pivot among rows within the feas_tol-relaxed
+                              step); 1: textbook minimum ratio.  Bland mode
+                              always uses the textbook rule. */
+  double feas_tol;         /* Harris relaxation; 0 = 1e-9 (FP64) / 1e-6 */
 } blpg_options;
 
 /* Per-LP outputs (host memory for blpg_solve_batch, device memory for

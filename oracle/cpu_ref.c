@@ -43,8 +43,11 @@ void oref_opts_init(oref_opts* o, int precision) {
   o->max_pivots = 0;
   o->bland_after = 64;
   o->opt_tol = precision == OREF_FP32 ? 1e-5 : 1e-9;
-  o->piv_tol = precision == OREF_FP32 ? 1e-6 : 1e-9;
+  o->piv_tol = precision == OREF_FP32 ? 1e-5 : 1e-7;
   o->phase1_tol = precision == OREF_FP32 ? 1e-4 : 1e-7;
+  o->deg_tol = precision == OREF_FP32 ? 1e-7 : 1e-12;
+  o->feas_tol = precision == OREF_FP32 ? 1e-6 : 1e-9;
+  o->harris = 1;
 }
 
 int oref_default_max_pivots(int m, int n) { return 50 * (m + n) + 1000; }

@@ -20,6 +20,9 @@ typedef struct {
   int bland_after; /* consecutive degenerate pivots before Bland's rule */
   int refactor_period;
   double opt_tol, piv_tol, phase1_tol;
+  double deg_tol; /* a pivot with ratio <= deg_tol counts as degenerate */
+  double feas_tol; /* Harris ratio-test relaxation */
+  int harris;      /* 1: Harris two-pass ratio test outside Bland mode */
 } oref_opts;
 
 void oref_opts_init(oref_opts* o, int precision);

@@ -26,8 +26,8 @@
  *     becomes the lowest eligible index (Bland's rule) for the rest of the
  *     solve, so degenerate LPs cannot cycle;
  *   - every elimination is one fused multiply-add, fma(-f, p_j, t_ij),
- *     applied to every row (the GPU kernels do the same, so the results
- *     are bit-identical).
+ *     applied to every row whose multiplier f is non-zero (the GPU kernels
+ *     do the same, so the results are bit-identical).
  */
 
 #define CAT2(a, b) a##b
@@ -61,17 +61,53 @@ static int FN(price)(const FN(tab_t) * t, int ncols, int bland, REAL opt_tol) {
   return q;
 }
 
-/* Leaving row for entering column q; -1 if no entry exceeds piv_tol. */
-static int FN(ratio)(const FN(tab_t) * t, int q, REAL piv_tol, REAL* theta_out) {
+/* Leaving row for entering column q; -1 if no entry exceeds piv_tol.
+ * Textbook rule (Bland mode): minimum ratio, ties by lowest basic variable.
+ * Harris rule (default): pass 1 bounds the step by the ratios relaxed by
+ * feas_tol, pass 2 takes the LARGEST pivot entry among rows whose ratio is
+ * within that bound (ties by lowest basic variable), so a tiny pivot never
+ * wins a tie of degenerate rows. */
+static int FN(ratio)(const FN(tab_t) * t, int q, REAL piv_tol, REAL feas_tol, int harris,
+                     REAL* theta_out) {
   int r = -1, rb = 0;
   REAL best = (REAL)0;
+  if (!harris) {
+    for (int i = 0; i < t->m; ++i) {
+      REAL a = TT(t, i, q);
+      if (!(a > piv_tol)) continue;
+      REAL rhs = TT(t, i, t->W - 1);
+      REAL th = rhs > (REAL)0 ? rhs / a : (REAL)0;
+      if (r < 0 || th < best || (th == best && t->basis[i] < rb)) {
+        r = i;
+        best = th;
+        rb = t->basis[i];
+      }
+    }
+    *theta_out = best;
+    return r;
+  }
+  REAL tmax = (REAL)0;
+  int any = 0;
+  for (int i = 0; i < t->m; ++i) {
+    REAL a = TT(t, i, q);
+    if (!(a > piv_tol)) continue;
+    REAL rhs = TT(t, i, t->W - 1);
+    REAL rr = rhs > (REAL)0 ? rhs : (REAL)0;
+    REAL th = (rr + feas_tol) / a;
+    if (!any || th < tmax) tmax = th;
+    any = 1;
+  }
+  if (!any) return -1;
+  REAL amax = (REAL)0;
   for (int i = 0; i < t->m; ++i) {
     REAL a = TT(t, i, q);
     if (!(a > piv_tol)) continue;
     REAL rhs = TT(t, i, t->W - 1);
     REAL th = rhs > (REAL)0 ? rhs / a : (REAL)0;
-    if (r < 0 || th < best || (th == best && t->basis[i] < rb)) {
+    if (!(th <= tmax)) continue;
+    if (r < 0 || a > amax || (a == amax && t->basis[i] < rb)) {
       r = i;
+      amax = a;
       best = th;
       rb = t->basis[i];
     }
@@ -90,6 +126,7 @@ static void FN(pivot)(FN(tab_t) * t, int r, int q, REAL* f) {
     if (i == r) continue;
     REAL* row = &TT(t, i, 0);
     const REAL fi = f[i];
+    if (fi == (REAL)0) continue; /* a zero multiplier leaves the row as it is */
     for (int j = 0; j < W; ++j) row[j] = FMA(-fi, pr[j], row[j]);
   }
   t->basis[r] = q;
@@ -104,11 +141,11 @@ static int FN(simplex_loop)(FN(tab_t) * t, int ncols, const oref_opts* o,
     if (q < 0) return OREF_OPT;
     if (*pivots >= o->max_pivots) return OREF_UNDEF;
     REAL theta;
-    int r = FN(ratio)(t, q, piv_tol, &theta);
+    int r = FN(ratio)(t, q, piv_tol, (REAL)o->feas_tol, o->harris && !*bland, &theta);
     if (r < 0) return OREF_UNBND;
     FN(pivot)(t, r, q, f);
     *pivots += 1;
-    if (theta == (REAL)0) {
+    if (theta <= (REAL)o->deg_tol) {
       *degen += 1;
       if (*degen > o->bland_after) *bland = 1;
     } else {
@@ -145,9 +182,12 @@ static int FN(solve_one)(int m, int n, const double* A, const double* b,
   int k = 0;
   for (int i = 0; i < m; ++i) {
     const REAL sgn = b[i] < 0 ? (REAL)-1 : (REAL)1;
-    for (int j = 0; j < n; ++j) TT(&t, i, j) = sgn * (REAL)A[(size_t)i * n + j];
+    for (int j = 0; j < n; ++j) {
+      const REAL av = (REAL)A[(size_t)i * n + j];
+      TT(&t, i, j) = b[i] < 0 ? -av : av;
+    }
     TT(&t, i, n + i) = sgn;
-    TT(&t, i, rhs) = sgn * (REAL)b[i];
+    TT(&t, i, rhs) = b[i] < 0 ? -(REAL)b[i] : (REAL)b[i];
     if (b[i] < 0) {
       TT(&t, i, n + m + k) = (REAL)1;
       t.basis[i] = n + m + k;

@@ -82,3 +82,92 @@ def solve(A, b, c):
             T[m][j] = -F(c[j])
     st = run(n + m)
     return st, T[m][W - 1]
+
+
+def _solve_int(M, rhs):
+    """Exact solve of the square rational system M x = rhs (fraction-free
+    Bareiss elimination on an integer-scaled copy).  None if singular."""
+    import math
+    n = len(M)
+    rows = []
+    for i in range(n):
+        vals = [F(v) for v in M[i]] + [F(rhs[i])]
+        den = 1
+        for v in vals:
+            den = den * v.denominator // math.gcd(den, v.denominator)
+        rows.append([v.numerator * (den // v.denominator) for v in vals])
+    prev = 1
+    for k in range(n):
+        p = next((i for i in range(k, n) if rows[i][k] != 0), None)
+        if p is None:
+            return None
+        rows[k], rows[p] = rows[p], rows[k]
+        rk = rows[k]
+        pk = rk[k]
+        for i in range(k + 1, n):
+            ri = rows[i]
+            f = ri[k]
+            if f == 0:
+                for j in range(k + 1, n + 1):
+                    ri[j] = ri[j] * pk // prev
+            else:
+                for j in range(k + 1, n + 1):
+                    ri[j] = (ri[j] * pk - f * rk[j]) // prev
+            ri[k] = 0
+        prev = pk
+    x = [F(0)] * n
+    for i in reversed(range(n)):
+        s = F(rows[i][n])
+        ri = rows[i]
+        for j in range(i + 1, n):
+            if ri[j]:
+                s -= ri[j] * x[j]
+        x[i] = s / ri[i]
+    return x
+
+
+def certify(A, b, c, basic):
+    """Exact optimality certificate of a basis for max c^T x, A x <= b, x >= 0.
+
+    `basic` lists m basic column ids (0..n-1 structural, n..n+m-1 slack).
+    Solves B x_B = b and B^T y = c_B exactly, then checks x_B >= 0 and every
+    reduced cost y^T a_j - c_j >= 0 (slack k: y_k >= 0).  Returns
+    (True, objective) when the basis is provably optimal, else (False, None)."""
+    m = len(A)
+    n = len(c)
+    basic = list(basic)
+    if len(basic) != m:
+        return False, None
+
+    def col(j):
+        if j < n:
+            return [A[i][j] for i in range(m)]
+        return [1 if i == j - n else 0 for i in range(m)]
+
+    cols = [col(j) for j in basic]
+    B = [[cols[k][i] for k in range(m)] for i in range(m)]
+    BT = [[cols[i][k] for k in range(m)] for i in range(m)]
+    cB = [c[j] if j < n else 0 for j in basic]
+    xB = _solve_int(B, list(b))
+    if xB is None or any(v < 0 for v in xB):
+        return False, None
+    y = _solve_int(BT, cB)
+    if y is None or any(v < 0 for v in y):
+        return False, None
+    Af = [[F(v) for v in row] for row in A]
+    for j in range(n):
+        dj = sum((y[i] * Af[i][j] for i in range(m) if Af[i][j] != 0), F(0)) - F(c[j])
+        if dj < 0:
+            return False, None
+    obj = sum((F(cB[k]) * xB[k] for k in range(m)), F(0))
+    return True, obj
+
+
+def unbounded_ray(A, c):
+    """A column with every entry <= 0 and a positive cost: x_j can grow
+    without bound, so the LP is unbounded (an exact certificate)."""
+    m = len(A)
+    for j in range(len(c)):
+        if c[j] > 0 and all(A[i][j] <= 0 for i in range(m)):
+            return True
+    return False

@@ -60,6 +60,8 @@ def lib(path: str = DEFAULT_LIB):
             "glp_get_status": (C.c_int, [vp]),
             "glp_get_obj_val": (C.c_double, [vp]),
             "glp_get_col_prim": (C.c_double, [vp, C.c_int]),
+            "glp_get_row_stat": (C.c_int, [vp, C.c_int]),
+            "glp_get_col_stat": (C.c_int, [vp, C.c_int]),
             "glp_term_out": (C.c_int, [C.c_int]),
             "glp_version": (C.c_char_p, []),
         }
@@ -71,10 +73,14 @@ def lib(path: str = DEFAULT_LIB):
     return _lib
 
 
+GLP_BS = 1  # basic (glp_get_row_stat / glp_get_col_stat)
+
+
 def solve(A, b, c, exact: bool = False, want_x: bool = False):
     """max c^T x, A x <= b, x >= 0 with glp_simplex (defaults) and, if
     `exact`, glp_exact from the final basis.  Returns a dict with status,
-    objective (and x)."""
+    objective, the final basis as column ids (0..n-1 structural, n+i for the
+    slack of row i) and optionally x."""
     L = lib()
     L.glp_term_out(GLP_OFF)
     A = np.asarray(A, dtype=np.float64)
@@ -97,6 +103,9 @@ def solve(A, b, c, exact: bool = False, want_x: bool = False):
         L.glp_load_matrix(P, ne, ia, ja, ar)
         ret = L.glp_simplex(P, None)
         out = {"ret": ret, "status": L.glp_get_status(P), "objective": L.glp_get_obj_val(P)}
+        basis = [j for j in range(n) if L.glp_get_col_stat(P, j + 1) == GLP_BS]
+        basis += [n + i for i in range(m) if L.glp_get_row_stat(P, i + 1) == GLP_BS]
+        out["basis"] = basis
         if exact:
             rete = L.glp_exact(P, None)
             out["exact_ret"] = rete

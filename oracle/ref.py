@@ -22,7 +22,8 @@ class Opts(C.Structure):
     _fields_ = [
         ("precision", C.c_int), ("max_pivots", C.c_int), ("bland_after", C.c_int),
         ("refactor_period", C.c_int), ("opt_tol", C.c_double), ("piv_tol", C.c_double),
-        ("phase1_tol", C.c_double),
+        ("phase1_tol", C.c_double), ("deg_tol", C.c_double), ("feas_tol", C.c_double),
+        ("harris", C.c_int),
     ]
 
 

@@ -38,6 +38,7 @@ class Options(C.Structure):
         ("refactor_period", C.c_int32), ("opt_tol", C.c_double), ("piv_tol", C.c_double),
         ("basis_hint", i32p), ("device", C.c_int32), ("use_graph", C.c_int32),
         ("threads_per_cta", C.c_int32), ("max_cluster", C.c_int32), ("min_cluster", C.c_int32),
+        ("cta_smem_budget", C.c_int32), ("ratio_rule", C.c_int32), ("feas_tol", C.c_double),
     ]
 
 

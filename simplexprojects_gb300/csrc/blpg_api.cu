@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -97,7 +98,9 @@ struct blpg_plan {
   int32_t *d_m = nullptr, *d_n = nullptr, *d_order = nullptr, *d_tickets = nullptr;
   int64_t *d_off = nullptr;  // offA | offb | offc | offx | offbasis
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_fork = nullptr;
+  std::vector<cudaStream_t> aux;      // one per class after the first
+  std::vector<cudaEvent_t> ev_join;
   cudaGraphExec_t gexec = nullptr;
   blpg::LpArgs graph_args{};
   int launches = 0;
@@ -116,6 +119,9 @@ static void release(blpg_plan* p) {
   cudaFree(p->d_off);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
   if (p->ev_out) cudaEventDestroy(p->ev_out);
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  for (auto e : p->ev_join) cudaEventDestroy(e);
+  for (auto st : p->aux) cudaStreamDestroy(st);
   if (p->stream) cudaStreamDestroy(p->stream);
 }
 
@@ -183,28 +189,41 @@ static int pick_threads(const Geom& g, int precision, int K, int override_nt) {
   return std::min(nt, kMaxThreads);
 }
 
+// Size classes.  Every LP gets the smallest cluster size K whose per-CTA
+// layout fits the CTA shared-memory budget (default: two CTAs per SM), so
+// large tableaux are spread over more SMs (shorter critical path) and all
+// classes have the same per-SM footprint.  One class per K; classes run
+// concurrently, each with a grid proportional to its share of the work.
 template <typename T>
 static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
   constexpr int V = dev::VecT<T>::V;
   const int elem = (int)sizeof(T);
+  int budget = p->opt.cta_smem_budget;
+  if (budget <= 0) {
+    std::lock_guard<std::mutex> lk(g_tuning.mu);
+    auto it = g_tuning.threads.find({p->precision * 16 + 15, 1});
+    budget = it != g_tuning.threads.end() ? it->second : (228 * 1024) / 2 - 1024;
+  }
+  budget = std::min(budget, max_smem);
+  const int min_cluster = std::max(1, std::min(p->opt.min_cluster, max_cluster));
   struct Item {
-    int lp, K, nt, smem, ldw;
+    int K, nl, ldw;
     double work;
   };
   std::vector<Item> items(p->count);
   for (int k = 0; k < p->count; ++k) {
     const int m = p->m[k], n = p->n[k], na = p->na[k];
     int chosen = 0;
-    const int min_cluster = std::max(1, std::min(p->opt.min_cluster, max_cluster));
-    for (int K = min_cluster; K <= max_cluster; K *= 2) {
-      Geom g(m, n, na, K, V);
-      Layout L(m, g.ldw, elem);
-      if (L.total <= max_smem && g.nl <= kMaxThreads) {
-        chosen = K;
-        items[k] = {k, K, pick_threads(g, p->precision, K, p->opt.threads_per_cta),
-                    L.total, g.ldw,
-                    (double)(m + 1) * (double)(n + m + 1) * (double)(m + n)};
-        break;
+    for (int pass = 0; pass < 2 && !chosen; ++pass) {
+      const int lim = pass == 0 ? budget : max_smem;
+      for (int K = min_cluster; K <= max_cluster; K *= 2) {
+        Geom g(m, n, na, K, V);
+        if (Layout(m, g.ldw, elem).total <= lim && g.nl <= kMaxThreads) {
+          chosen = K;
+          items[k] = {K, g.nl, g.ldw,
+                      (double)(m + 1) * (double)(n + m + na + 1) * (double)(m + n)};
+          break;
+        }
       }
     }
     if (!chosen)
@@ -212,27 +231,17 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
                   "LP %d (m=%d, n=%d) needs more than %d CTAs of shared memory", k, m,
                   n, max_cluster);
   }
-  // Group by (K, nt, occupancy level): the class is sized for its largest
-  // member, which keeps the member's own occupancy.
-  std::map<std::tuple<int, int, int>, std::vector<int>> groups;
-  for (auto& it : items) {
-    int per_sm = std::max(1, (228 * 1024) / (it.smem + 1024));
-    per_sm = std::min(per_sm, 2048 / it.nt);
-    groups[{it.K, it.nt, per_sm}].push_back(it.lp);
-  }
+  std::map<int, std::vector<int>> groups;
+  for (int k = 0; k < p->count; ++k) groups[items[k].K].push_back(k);
   p->classes.clear();
   p->order.clear();
+  double total_work = 0;
+  for (auto& it : items) total_work += it.work;
   for (auto& kv : groups) {
-    const int K = std::get<0>(kv.first), nt = std::get<1>(kv.first);
-    const int per_sm_key = std::get<2>(kv.first);
-    // smem budget of the bucket: keep the members' occupancy level
-    const int bucket_smem = std::min(max_smem, (228 * 1024) / per_sm_key - 1024);
     auto& lps = kv.second;
     std::stable_sort(lps.begin(), lps.end(),
                      [&](int a, int b) { return items[a].work > items[b].work; });
-    // Greedy split: a class's layout is sized by its largest m and largest
-    // ldw, which may come from different members; start a new class when
-    // the combined layout would not fit.
+    // split only if the combined (max m, max ldw) layout would overflow
     std::vector<ClassPlan> parts;
     std::vector<std::vector<int>> members;
     for (int lp : lps) {
@@ -241,30 +250,37 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
         ClassPlan& c = parts[ci];
         const int mm = std::max(c.max_m, p->m[lp]);
         const int ll = std::max(c.max_ldw, items[lp].ldw);
-        if (Layout(mm, ll, elem).total <= std::max(bucket_smem, items[lp].smem) &&
-            Layout(mm, ll, elem).total <= max_smem) {
+        const int lim = std::max(budget, Layout(p->m[lp], items[lp].ldw, elem).total);
+        if (Layout(mm, ll, elem).total <= std::min(lim, max_smem)) {
           c.max_m = mm;
           c.max_ldw = ll;
           c.max_na = std::max(c.max_na, p->na[lp]);
           c.work += items[lp].work;
+          c.nt = std::max(c.nt, items[lp].nl);
           members[ci].push_back(lp);
           placed = true;
         }
       }
       if (!placed) {
         ClassPlan c;
-        c.K = K;
-        c.nt = nt;
+        c.K = kv.first;
         c.max_m = p->m[lp];
         c.max_ldw = items[lp].ldw;
         c.max_na = p->na[lp];
         c.work = items[lp].work;
+        c.nt = items[lp].nl;
         parts.push_back(c);
         members.push_back({lp});
       }
     }
     for (size_t ci = 0; ci < parts.size(); ++ci) {
       ClassPlan c = parts[ci];
+      Geom gmax(c.max_m, 1, 0, 1, V);
+      (void)gmax;
+      // threads: every member's row of vector lanes at least once
+      Geom gl(0, 0, 0, 1, V);
+      gl.nl = c.nt;  // c.nt holds the widest member's lane count here
+      c.nt = pick_threads(gl, p->precision, c.K, p->opt.threads_per_cta);
       c.smem = Layout(c.max_m, c.max_ldw, elem).total;
       c.count = (int)members[ci].size();
       c.order_off = (int)p->order.size();
@@ -276,47 +292,67 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
       if (slots <= 0)
         return fail(BLPG_ETOOBIG, "class K=%d nt=%d smem=%d cannot be resident", c.K,
                     c.nt, c.smem);
-      c.grid = std::min(slots, c.count) * c.K;
+      // share of the GPU proportional to the class's work (classes co-run)
+      const double share = total_work > 0 ? c.work / total_work : 1.0;
+      int want = (int)std::ceil(share * slots);
+      want = std::max(1, std::min(want, slots));
+      c.grid = std::min(want, c.count) * c.K;
       p->classes.push_back(c);
     }
   }
-  // heaviest class first
   std::stable_sort(p->classes.begin(), p->classes.end(),
                    [](const ClassPlan& a, const ClassPlan& b) { return a.work > b.work; });
   return BLPG_OK;
 }
 
 template <typename T>
+static int launch_one(blpg_plan* p, size_t ci, const LpArgs& args, cudaStream_t s) {
+  const ClassPlan& c = p->classes[ci];
+  ClassArgs ca;
+  ca.order = p->d_order + c.order_off;
+  ca.count = c.count;
+  ca.ticket = p->d_tickets + ci;
+  ca.K = c.K;
+  ca.max_m = c.max_m;
+  ca.max_ldw = c.max_ldw;
+  ca.max_na = c.max_na;
+  if (c.K == 1) {
+    dev::solve_kernel<T, false><<<c.grid, c.nt, c.smem, s>>>(args, ca);
+    CK(cudaGetLastError());
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = c.K;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(c.grid, 1, 1);
+    cfg.blockDim = dim3(c.nt, 1, 1);
+    cfg.dynamicSmemBytes = c.smem;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    CK(cudaLaunchKernelEx(&cfg, dev::solve_kernel<T, true>, args, ca));
+  }
+  return BLPG_OK;
+}
+
+// Queue reset, then every class on its own stream (fork/join through
+// events, so a captured graph has one parallel branch per class).
+template <typename T>
 static int launch_classes(blpg_plan* p, const LpArgs& args, cudaStream_t s) {
-  CK(cudaMemsetAsync(p->d_tickets, 0, sizeof(int32_t) * p->classes.size(), s));
-  for (size_t ci = 0; ci < p->classes.size(); ++ci) {
-    const ClassPlan& c = p->classes[ci];
-    ClassArgs ca;
-    ca.order = p->d_order + c.order_off;
-    ca.count = c.count;
-    ca.ticket = p->d_tickets + ci;
-    ca.K = c.K;
-    ca.max_m = c.max_m;
-    ca.max_ldw = c.max_ldw;
-    ca.max_na = c.max_na;
-    if (c.K == 1) {
-      dev::solve_kernel<T, false><<<c.grid, c.nt, c.smem, s>>>(args, ca);
-      CK(cudaGetLastError());
-    } else {
-      cudaLaunchConfig_t cfg = {};
-      cudaLaunchAttribute at[1];
-      at[0].id = cudaLaunchAttributeClusterDimension;
-      at[0].val.clusterDim.x = c.K;
-      at[0].val.clusterDim.y = 1;
-      at[0].val.clusterDim.z = 1;
-      cfg.gridDim = dim3(c.grid, 1, 1);
-      cfg.blockDim = dim3(c.nt, 1, 1);
-      cfg.dynamicSmemBytes = c.smem;
-      cfg.stream = s;
-      cfg.attrs = at;
-      cfg.numAttrs = 1;
-      CK(cudaLaunchKernelEx(&cfg, dev::solve_kernel<T, true>, args, ca));
-    }
+  CK(cudaMemsetAsync(p->d_tickets, 0, sizeof(int32_t) * std::max<size_t>(1, p->classes.size()), s));
+  const size_t nc = p->classes.size();
+  if (nc == 0) return BLPG_OK;
+  CK(cudaEventRecord(p->ev_fork, s));
+  for (size_t ci = 1; ci < nc; ++ci) CK(cudaStreamWaitEvent(p->aux[ci - 1], p->ev_fork, 0));
+  for (size_t ci = 0; ci < nc; ++ci) {
+    int rc = launch_one<T>(p, ci, args, ci == 0 ? s : p->aux[ci - 1]);
+    if (rc) return rc;
+  }
+  for (size_t ci = 1; ci < nc; ++ci) {
+    CK(cudaEventRecord(p->ev_join[ci - 1], p->aux[ci - 1]));
+    CK(cudaStreamWaitEvent(s, p->ev_join[ci - 1], 0));
   }
   return BLPG_OK;
 }
@@ -365,6 +401,10 @@ extern "C" int32_t blpg_set_tuning(const char* json) {
     if (std::sscanf(key.c_str(), "fp64_k%d", &K) == 1) prec = BLPG_FP64;
     else if (std::sscanf(key.c_str(), "fp32_k%d", &K) == 1) prec = BLPG_FP32;
     if (prec >= 0 && val > 0 && val <= 1024) g_tuning.threads[{prec * 16 + K, 0}] = val;
+    if (std::sscanf(key.c_str(), "fp64_smem%d", &K) == 1 && val > 0)
+      g_tuning.threads[{BLPG_FP64 * 16 + 15, 1}] = val;
+    if (std::sscanf(key.c_str(), "fp32_smem%d", &K) == 1 && val > 0)
+      g_tuning.threads[{BLPG_FP32 * 16 + 15, 1}] = val;
     s = colon + 1;
   }
   return BLPG_OK;
@@ -459,6 +499,15 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
   CKF(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
   CKF(cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming));
   CKF(cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming));
+  CKF(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+  for (size_t ci = 1; ci < p->classes.size(); ++ci) {
+    cudaStream_t st;
+    cudaEvent_t ev;
+    CKF(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    p->aux.push_back(st);
+    CKF(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    p->ev_join.push_back(ev);
+  }
   const size_t Nn = std::max(1, N);
   CKF(cudaMalloc(&p->d_m, sizeof(int32_t) * Nn));
   CKF(cudaMalloc(&p->d_n, sizeof(int32_t) * Nn));
@@ -512,8 +561,11 @@ extern "C" int32_t blpg_plan_execute(blpg_plan* p, const double* dA, const doubl
   a.basis = out->basis;
   const bool fp32 = p->precision == BLPG_FP32;
   a.opt_tol = p->opt.opt_tol > 0 ? p->opt.opt_tol : (fp32 ? 1e-5 : 1e-9);
-  a.piv_tol = p->opt.piv_tol > 0 ? p->opt.piv_tol : (fp32 ? 1e-6 : 1e-9);
+  a.piv_tol = p->opt.piv_tol > 0 ? p->opt.piv_tol : (fp32 ? 1e-5 : 1e-7);
+  a.feas_tol = p->opt.feas_tol > 0 ? p->opt.feas_tol : (fp32 ? 1e-6 : 1e-9);
   a.phase1_tol = fp32 ? 1e-4 : 1e-7;
+  a.deg_tol = fp32 ? 1e-7 : 1e-12;
+  a.harris = p->opt.ratio_rule == 1 ? 0 : 1;
   a.max_pivots = p->opt.max_pivots;
   a.bland_after = p->opt.bland_after > 0 ? p->opt.bland_after : 64;
   CK(cudaEventRecord(p->ev_in, user));

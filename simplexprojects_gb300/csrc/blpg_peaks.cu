@@ -15,21 +15,46 @@
 
 namespace {
 
+__device__ __forceinline__ float4 lds4(unsigned addr) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ void sts4(unsigned addr, float4 v) {
+  asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(v.x), "f"(v.y),
+               "f"(v.z), "f"(v.w)
+               : "memory");
+}
+
+// Volatile 16-byte shared loads and stores (they cannot be forwarded or
+// removed), four independent streams per thread, bank-conflict free.
 __global__ void __launch_bounds__(512) smem_probe(float* sink, int iters) {
-  extern __shared__ float4 buf[];  // 512 float4 per CTA
+  extern __shared__ float4 buf[];  // 2048 float4 (32 KB) per CTA
   const int t = threadIdx.x;
-  buf[t] = make_float4(t, t + 1, t + 2, t + 3);
+  for (int i = t; i < 2048; i += 512) buf[i] = make_float4(i, i + 1, i + 2, i + 3);
   __syncthreads();
-  float4 acc = make_float4(0, 0, 0, 0);
-  int idx = t;
+  const unsigned base_addr = (unsigned)__cvta_generic_to_shared(buf);
+  float acc = 0.f;
   for (int it = 0; it < iters; ++it) {
-    float4 v = buf[idx];
-    acc.x += v.x;
-    v.y += 1.0f;
-    buf[idx] = v;
-    idx = (idx + 32) & 511;
+    const int base = (it & 3) * 512;
+    const unsigned a0 = base_addr + 16u * ((base + t) & 2047);
+    const unsigned a1 = base_addr + 16u * ((base + 512 + t) & 2047);
+    const unsigned a2 = base_addr + 16u * ((base + 1024 + t) & 2047);
+    const unsigned a3 = base_addr + 16u * ((base + 1536 + t) & 2047);
+    float4 v0 = lds4(a0), v1 = lds4(a1), v2 = lds4(a2), v3 = lds4(a3);
+    acc += v0.x + v1.y + v2.z + v3.w;
+    v0.y += 1.f;
+    v1.z += 1.f;
+    v2.w += 1.f;
+    v3.x += 1.f;
+    sts4(a2, v0);
+    sts4(a3, v1);
+    sts4(a0, v2);
+    sts4(a1, v3);
   }
-  if (acc.x == -1.0f) sink[t] = acc.y;
+  if (acc == -1.0f) sink[t] = acc;
 }
 
 template <typename T>
@@ -73,14 +98,14 @@ extern "C" int32_t blpg_measure_peaks(int32_t device, double* smem_gbs, double* 
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   double best_smem = 0, best64 = 0, best32 = 0;
-  const int smem_iters = 1 << 14;
+  const int smem_iters = 1 << 12;
   const int blocks = sms * 4;
   for (int rep = 0; rep < 4; ++rep) {
     cudaEventRecord(e0);
-    smem_probe<<<blocks, 512, 512 * sizeof(float4)>>>(sink, smem_iters);
+    smem_probe<<<blocks, 512, 2048 * sizeof(float4)>>>(sink, smem_iters);
     cudaEventRecord(e1);
     cudaEventSynchronize(e1);
-    double bytes = (double)blocks * 512 * smem_iters * 32.0;  // 16 B load + 16 B store
+    double bytes = (double)blocks * 512 * smem_iters * 128.0;  // 4 x (16 B load + 16 B store)
     double gbs = bytes / (time_ms(e0, e1) * 1e-3) / 1e9;
     if (rep > 0 && gbs > best_smem) best_smem = gbs;
   }

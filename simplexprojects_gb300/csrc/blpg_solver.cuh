@@ -58,6 +58,9 @@ struct LpArgs {
   double opt_tol;
   double piv_tol;
   double phase1_tol;
+  double feas_tol;  // Harris ratio-test relaxation
+  double deg_tol;   // a step <= deg_tol counts as degenerate
+  int32_t harris;   // 1: Harris two-pass ratio test outside Bland mode
   int32_t max_pivots;  // <= 0: 50 (m + n) + 1000
   int32_t bland_after;
 };
@@ -121,7 +124,7 @@ struct Layout {
     basis = off;
     off += round_up(mp1 * 4, 16);
     red = off;
-    off += 2 * 32 * 16;
+    off += 3 * 32 * 16;  // three argmin scratch buffers (pricing, ratio, Harris)
     state = off;
     off += 64;
     total = off;
@@ -193,6 +196,14 @@ __device__ __forceinline__ Key ratio_key(double th, int bid, int row) {
 __device__ __forceinline__ Key ratio_key(float th, int bid, int row) {
   return Key{__float_as_uint(th), 0u, (unsigned)bid, (unsigned)row};
 }
+// Largest positive value first: ~bits is decreasing in a positive value.
+__device__ __forceinline__ Key big_key(double a, int bid, int row) {
+  unsigned long long u = ~(unsigned long long)__double_as_longlong(a);
+  return Key{(unsigned)(u >> 32), (unsigned)u, (unsigned)bid, (unsigned)row};
+}
+__device__ __forceinline__ Key big_key(float a, int bid, int row) {
+  return Key{~__float_as_uint(a), 0u, (unsigned)bid, (unsigned)row};
+}
 __device__ __forceinline__ double key_theta(const Key& k, double) {
   return __hiloint2double((int)k.w0, (int)k.w1);
 }
@@ -249,11 +260,14 @@ struct Solver {
 
   unsigned char* smem;
   T* tab;
-  T* col[2];
+  T* col0;
+  T* col1;
+  __device__ T* colbuf(int k) const { return k ? col1 : col0; }
   T* rhsx;
   int* basis;
   Key* redP;
   Key* redR;
+  Key* redH;
   SharedState* sh;
   int K, rank;
 
@@ -309,19 +323,59 @@ struct Solver {
     }
   }
 
-  // Ratio test on the owner CTA: every thread returns the winning key.
-  __device__ Key ratio(const Geom& g, const T* colx, T piv_tol) {
+  // Ratio test on the owner CTA: every thread returns the winning key
+  // (payload = row) and theta.  Textbook rule: minimum ratio, ties by lowest
+  // basic variable.  Harris rule: pass 1 bounds the step by the ratios
+  // relaxed by feas_tol, pass 2 takes the largest pivot entry among rows
+  // within the bound (ties by lowest basic variable).  The oracle's ratio()
+  // performs the same operations.
+  __device__ Key ratio(const Geom& g, const T* colx, T piv_tol, T feas_tol, bool harris,
+                       T& theta) {
     Key k = key_none();
+    if (!harris) {
+      for (int i = threadIdx.x; i < g.m; i += blockDim.x) {
+        const T a = colx[i];
+        if (a > piv_tol) {
+          const T rh = rhsx[i];
+          const T th = rh > T(0) ? rh / a : T(0);
+          Key kk = ratio_key(th, basis[i], i);
+          if (key_less(kk, k)) k = kk;
+        }
+      }
+      k = block_min(k, redR);
+      theta = key_theta(k, T(0));
+      return k;
+    }
+    for (int i = threadIdx.x; i < g.m; i += blockDim.x) {
+      const T a = colx[i];
+      if (a > piv_tol) {
+        const T rh = rhsx[i];
+        const T rr = rh > T(0) ? rh : T(0);
+        const T th1 = (rr + feas_tol) / a;
+        Key kk = ratio_key(th1, 0, i);
+        if (key_less(kk, k)) k = kk;
+      }
+    }
+    k = block_min(k, redR);
+    if (k.w2 == ~0u) return k;
+    const T tmax = key_theta(k, T(0));
+    Key k2 = key_none();
     for (int i = threadIdx.x; i < g.m; i += blockDim.x) {
       const T a = colx[i];
       if (a > piv_tol) {
         const T rh = rhsx[i];
         const T th = rh > T(0) ? rh / a : T(0);
-        Key kk = ratio_key(th, basis[i], i);
-        if (key_less(kk, k)) k = kk;
+        if (th <= tmax) {
+          Key kk = big_key(a, basis[i], i);
+          if (key_less(kk, k2)) k2 = kk;
+        }
       }
     }
-    return block_min(k, redR);
+    k2 = block_min(k2, redH);
+    const int r = (int)k2.w3;
+    const T a = colx[r], rh = rhsx[r];
+    theta = rh > T(0) ? rh / a : T(0);
+    return k2;
   }
 
   // Pivot row scale + objective-row update + pricing of the next column.
@@ -337,8 +391,10 @@ struct Solver {
       p = v_div(p, piv);
       *reinterpret_cast<VT*>(prow + v * V) = p;
       VT d = *reinterpret_cast<const VT*>(drow + v * V);
-      d = v_fma(dq, p, d);
-      *reinterpret_cast<VT*>(drow + v * V) = d;
+      if (dq != T(0)) {
+        d = v_fma(dq, p, d);
+        *reinterpret_cast<VT*>(drow + v * V) = d;
+      }
 #pragma unroll
       for (int e = 0; e < V; ++e) {
         const int lj = v * V + e;
@@ -373,8 +429,12 @@ struct Solver {
       if (i != r) {
         const T f = pcol[i];
         VT* tp = reinterpret_cast<VT*>(tab + (size_t)i * g.ldw + lane * V);
-        t = v_fma(f, p, *tp);
-        *tp = t;
+        if (f != T(0)) {
+          t = v_fma(f, p, *tp);
+          *tp = t;
+        } else {
+          t = *tp;  // fma(-0, p, t) would only flip the sign of a zero t
+        }
       } else {
         t = p;
       }
@@ -388,22 +448,22 @@ struct Solver {
   // simplex_loop).  Pricing covers global columns [0, price_cols).
   __device__ int loop(const Geom& g, int c0, int lc, int price_cols, const LpArgs& a,
                       int max_piv, int& pivots, bool& bland, int& degen, int& cur) {
-    const T opt_tol = (T)a.opt_tol, piv_tol = (T)a.piv_tol;
+    const T opt_tol = (T)a.opt_tol, piv_tol = (T)a.piv_tol, feas_tol = (T)a.feas_tol;
+    const T deg_tol = (T)a.deg_tol;
     Key kq = price_only(g, c0, lc, bland, opt_tol, price_cols);
     int q = kq.w2 == ~0u ? -1 : (int)kq.w2;
     if (q < 0) return kOpt;
     if (pivots >= max_piv) return kUndef;
     int owner = q / g.cw;
-    if (owner == rank) extract(g, q, c0, col[cur]);
+    if (owner == rank) extract(g, q, c0, colbuf(cur));
     __syncthreads();
     for (;;) {
       // A: ratio test on the owner of q
       int r = -1;
       T theta = T(0);
       if (owner == rank) {
-        Key kr = ratio(g, col[cur], piv_tol);
+        Key kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta);
         r = kr.w2 == ~0u ? -1 : (int)kr.w3;
-        theta = key_theta(kr, T(0));
         if (CLUSTER && threadIdx.x == 0) {
           sh->r = r;
           sh->theta = (double)theta;
@@ -419,23 +479,23 @@ struct Solver {
       }
       if (r < 0) return kUnbnd;
       if (CLUSTER && owner != rank) {
-        const T* src = remote(col[cur], owner);
-        for (int i = threadIdx.x; i <= g.m; i += blockDim.x) col[cur][i] = src[i];
+        const T* src = remote(colbuf(cur), owner);
+        for (int i = threadIdx.x; i <= g.m; i += blockDim.x) colbuf(cur)[i] = src[i];
         __syncthreads();
       }
-      if (theta == T(0)) {
+      if (theta <= deg_tol) {
         if (++degen > a.bland_after) bland = true;
       } else {
         degen = 0;
       }
       // C: pivot row, objective row, next pricing (cluster barrier B2 inside)
-      const T* pcol = col[cur];
+      const T* pcol = colbuf(cur);
       Key kn = pivot_rows(g, r, pcol, c0, lc, bland, opt_tol, price_cols);
       const int qn = kn.w2 == ~0u ? -1 : (int)kn.w2;
       const int owner_n = qn >= 0 ? qn / g.cw : -1;
       if (threadIdx.x == 0) basis[r] = q;
       // D: body update, extraction of the next pivot column
-      update_body(g, r, pcol, qn, owner_n, c0, col[cur ^ 1]);
+      update_body(g, r, pcol, qn, owner_n, c0, colbuf(cur ^ 1));
       __syncthreads();
       cur ^= 1;
       ++pivots;
@@ -501,20 +561,20 @@ struct Solver {
       if (k.w2 == ~0u) continue;  // redundant row: artificial stays basic at 0
       const int q = (int)k.w2;
       const int owner = q / g.cw;
-      if (owner == rank) extract(g, q, c0, col[cur]);
+      if (owner == rank) extract(g, q, c0, colbuf(cur));
       if (CLUSTER) {
         csync();
         if (owner != rank) {
-          const T* src = remote(col[cur], owner);
-          for (int e = threadIdx.x; e <= g.m; e += blockDim.x) col[cur][e] = src[e];
+          const T* src = remote(colbuf(cur), owner);
+          for (int e = threadIdx.x; e <= g.m; e += blockDim.x) colbuf(cur)[e] = src[e];
         }
       }
       __syncthreads();
-      const T* pcol = col[cur];
+      const T* pcol = colbuf(cur);
       // pivot without pricing: reuse pivot_rows with an impossible tolerance
       pivot_rows(g, i, pcol, c0, lc, false, T(0), 0);
       if (threadIdx.x == 0) basis[i] = q;
-      update_body(g, i, pcol, -1, -1, c0, col[cur ^ 1]);
+      update_body(g, i, pcol, -1, -1, c0, colbuf(cur ^ 1));
       __syncthreads();
       if (CLUSTER) csync();  // column copies done before the owner's next extract
       ++pivots;
@@ -572,7 +632,10 @@ struct Solver {
             const int j = c0 + lj;
             if (i < m) {
               if (j < n)
-                v = sgn * (T)A[(size_t)i * n + j];
+                {
+                const T av = (T)A[(size_t)i * n + j];
+                v = neg ? -av : av;
+              }
               else if (j < n + m)
                 v = (j - n == i) ? sgn : T(0);
               else
@@ -581,7 +644,10 @@ struct Solver {
               v = -(T)c[j];
             }
           } else if (lj == g.cw && i < m) {
-            v = sgn * (T)b[i];
+            {
+            const T bv = (T)b[i];
+            v = neg ? -bv : bv;
+          }
           }
           row[lj] = v;
         }
@@ -656,12 +722,13 @@ __global__ void __launch_bounds__(512, 1) solve_kernel(const LpArgs a, const Cla
   const Layout L(ca.max_m, ca.max_ldw, (int)sizeof(T));
   s.smem = smem_raw;
   s.tab = reinterpret_cast<T*>(smem_raw + L.tab);
-  s.col[0] = reinterpret_cast<T*>(smem_raw + L.colA);
-  s.col[1] = reinterpret_cast<T*>(smem_raw + L.colB);
+  s.col0 = reinterpret_cast<T*>(smem_raw + L.colA);
+  s.col1 = reinterpret_cast<T*>(smem_raw + L.colB);
   s.rhsx = reinterpret_cast<T*>(smem_raw + L.rhsx);
   s.basis = reinterpret_cast<int*>(smem_raw + L.basis);
   s.redP = reinterpret_cast<Key*>(smem_raw + L.red);
   s.redR = s.redP + 32;
+  s.redH = s.redP + 64;
   s.sh = reinterpret_cast<SharedState*>(smem_raw + L.state);
   s.K = ca.K;
   s.rank = CLUSTER ? (int)cg::this_cluster().block_rank() : 0;

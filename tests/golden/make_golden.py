@@ -2,18 +2,22 @@
 
 Runs in the x86 container only: it calls GLPK 4.45 from the reference's
 prebuilt lib/libglpk.so.0.30.0 (glp_simplex with default parameters, as the
-reference's glpk_lp_solver.cpp:435-454, and glp_exact over GMP rationals as
-the exact judge).  The LP data itself is not stored: every fixture names the
-workload kind, seed and LP indices, and a SHA-256 of the generated A, b, c so
-that a change of the generator is caught.
+reference's glpk_lp_solver.cpp:435-454).  The exact verdict of each LP is an
+exact certificate: GLPK's final basis is proven optimal by solving
+B x_B = b and B^T y = c_B in rational arithmetic and checking the signs of
+x_B and of every reduced cost (oracle/exact.py), or unboundedness is proven
+by a column with no positive entry and a positive cost; glp_exact (GMP) is
+used for the small hand LPs.  The LP data itself is not stored: every
+fixture names the workload kind, seed and LP indices, and a SHA-256 of the
+generated A, b, c so that a change of the generator is caught.
 
 Fixtures:
   workloads.json   per workload kind 0..4, a sample of seeded LPs with GLPK's
-                   status/objective and glp_exact's status/objective
+                   status/objective and the exact status/objective
   known.json       the reference's hand LPs (parseBenchmark.cpp:128-319,
                    GPU_Tester.cu:80-86) and the 8 Netlib LPs it ships
                    (benchmarks/*.txt, listed optima parseBenchmark.cpp:15-25),
-                   solved by GLPK and glp_exact
+                   solved by GLPK with exact verdicts
 
 Usage:  python tests/golden/make_golden.py [--quick]
 """
@@ -91,16 +95,38 @@ def fingerprint(batch) -> str:
 
 
 def _solve_one(args):
+    """GLPK (glp_simplex, default parameters) and an exact verdict: the exact
+    optimality certificate of GLPK's final basis (oracle/exact.py: rational
+    solves of B x_B = b and B^T y = c_B, sign checks of x_B and of every
+    reduced cost), an exact unbounded ray, or glp_exact for small LPs."""
     A, b, c = args
-    from oracle import glpk
-    r = glpk.solve(np.asarray(A), np.asarray(b), np.asarray(c), exact=True)
-    return {k: r[k] for k in ("status", "objective", "exact_status", "exact_objective")}
+    from oracle import exact, glpk
+    m = len(A)
+    small = m <= 40
+    r = glpk.solve(np.asarray(A), np.asarray(b), np.asarray(c), exact=small)
+    out = {"status": r["status"], "objective": r["objective"]}
+    est, eobj, how = None, None, None
+    if r["status"] == glpk.GLP_OPT:
+        ok, obj = exact.certify(A, b, c, r["basis"])
+        if ok:
+            est, eobj, how = 5, float(obj), "certificate"
+    if est is None and r["status"] == glpk.GLP_UNBND and exact.unbounded_ray(A, c):
+        est, how = 6, "ray"
+    if est is None and small:
+        est, eobj, how = r["exact_status"], r["exact_objective"], "glp_exact"
+    if est is None:
+        st, obj = exact.solve(A, b, c) if m <= 60 else (None, None)
+        if st is not None:
+            est, eobj, how = st, (float(obj) if obj is not None else None), "fraction_simplex"
+    out.update(exact_status=est, exact_objective=eobj, exact_method=how)
+    return out
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true", help="smaller samples (smoke the script)")
     ap.add_argument("--procs", type=int, default=8)
+    ap.add_argument("--known-only", action="store_true", help="regenerate known.json only")
     args = ap.parse_args()
     import simplexprojects_gb300 as sp
     from oracle import glpk
@@ -110,7 +136,7 @@ def main():
     t0 = time.time()
     out = {"seed": SEED, "glpk_version": glpk.lib().glp_version().decode(), "workloads": {}}
     with ctx.Pool(args.procs) as pool:
-        for kind, (first, count) in SAMPLES.items():
+        for kind, (first, count) in ({} if args.known_only else SAMPLES).items():
             if args.quick:
                 count = min(count, 4)
             batch = sp.generate(kind, count, seed=SEED, first=first)
@@ -121,7 +147,8 @@ def main():
                 "m": batch.m.tolist(), "n": batch.n.tolist(), "lps": res,
             }
             print(f"kind {kind}: {count} LPs, {time.time() - t0:.0f}s", flush=True)
-        (HERE / "workloads.json").write_text(json.dumps(out, indent=1))
+        if not args.known_only:
+            (HERE / "workloads.json").write_text(json.dumps(out, indent=1))
         known = {"hand": {}, "netlib": {}}
         for name, (A, b, c, stated) in hand_lps().items():
             r = _solve_one((A, b, c))
