@@ -174,6 +174,33 @@ int32_t blpg_set_tuning(const char* json_text);
 const char* blpg_last_error(void);
 const char* blpg_version(void);
 
+/* Solve without allocating any memory.  No counterpart in the reference (its
+ * ComputeLP allocates device memory on every call).  For callers that cannot
+ * call cudaMalloc — code running inside a memory pool or arena it does not
+ * own, or a host framework that hands all device memory to its own allocator:
+ * every input and output is a caller-provided DEVICE pointer, and the kernel's
+ * scratch (the work-queue ticket and the LP order it hands out) lives in a
+ * fixed array compiled into the library (about 1 MiB, held on every GPU that
+ * loads the library until exit).
+ *  - count <= 262144 LPs per call (larger counts: BLPG_EINVAL, no GPU work);
+ *  - max_m / max_n bound every LP's shape (they size shared memory); offsets
+ *    are required (device arrays, as blpg_batch); x (nullable) uses off_c;
+ *  - single-phase LPs only: an LP with b_i < 0 or outside the bounds gets
+ *    status BLPG_UNDEF and pivots -1;
+ *  - the first call on a device does set-up (looks up the scratch address,
+ *    sets kernel attributes): make it before any stream capture;
+ *  - all calls share the scratch array (each call resets it first), so calls
+ *    whose GPU work overlaps race: serialise them;
+ *  - asynchronous on `stream`; default tolerances and rules of blpg_options. */
+int32_t blpg_solve_noalloc(int32_t count, int32_t max_m, int32_t max_n,
+                           const int32_t* d_m, const int32_t* d_n,
+                           const int64_t* d_off_A, const int64_t* d_off_b,
+                           const int64_t* d_off_c, const double* dA,
+                           const double* db, const double* dc,
+                           int32_t precision, int32_t* d_status,
+                           double* d_objective, double* d_x, int32_t* d_pivots,
+                           void* stream);
+
 /* Roofline denominators of the pivot kernels, timed on `device` by synthetic
  * kernels: shared-memory bandwidth (GB/s, bytes read + written) and FP64 /
  * FP32 FMA throughput (TFLOP/s, 2 flops per FMA).  No reference counterpart

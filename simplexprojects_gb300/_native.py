@@ -63,6 +63,8 @@ SIGNATURES = {
     "blpg_last_error": (C.c_char_p, []),
     "blpg_version": (C.c_char_p, []),
     "blpg_measure_peaks": (C.c_int32, [C.c_int32, f64p, f64p, f64p]),
+    "blpg_solve_noalloc": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32] + [C.c_void_p] * 8
+                           + [C.c_int32] + [C.c_void_p] * 5),
     "blpg_read_abc": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, i32p, i32p, f64p, f64p, f64p]),
     "blpg_gen_shapes": (C.c_int64, [C.c_int32, C.c_int64, C.c_int32, C.c_uint64, i32p, i32p, i32p]),
     "blpg_gen_fill": (C.c_int32, [C.c_int32, C.c_int64, C.c_int32, C.c_uint64, i32p, i32p, f64p,

@@ -45,6 +45,7 @@ def _nvcc() -> str:
 SOURCES = [
     ("blpg_api.cu", ["--fmad=false"]),
     ("blpg_peaks.cu", []),
+    ("blpg_noalloc.cu", ["--fmad=false"]),
     ("blpg_gen.cpp", []),
 ]
 
