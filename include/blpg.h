@@ -94,13 +94,20 @@ typedef struct blpg_options {
   int32_t max_pivots;      /* per-LP pivot cap; 0 = 50 * (m + n) + 1000 */
   int32_t bland_after;     /* consecutive degenerate pivots before Bland's
                               rule takes over for the rest of the LP; 0 = 64 */
-  int32_t refactor_period; /* FP32 only: FP64 refresh of x_B and reduced costs
-                              every k pivots; 0 = at termination only */
+  int32_t refactor_period; /* FP32 only: FP64 refresh of x_B, the duals and
+                              the reduced costs every k pivots; 0 = only at
+                              termination (always done there) */
   double opt_tol;          /* reduced-cost tolerance; 0 = 1e-9 (FP64) / 1e-5 */
   double piv_tol;          /* pivot tolerance;       0 = 1e-7 (FP64) / 1e-5 */
-  const int32_t* basis_hint; /* nullable warm start: per LP, m[k] column ids
-                                (0..n-1 structural, n..n+m-1 slack), packed
-                                in LP order; see blpg_solve_batch */
+  const int32_t* basis_hint; /* nullable warm start (host memory for
+                                blpg_solve_batch): per LP, m[k] column ids
+                                (0..n-1 structural, n..n+m-1 slack), packed in
+                                LP order.  The hinted structural columns are
+                                pivoted in; the LP is then finished by primal
+                                simplex (hinted basis primal feasible), dual
+                                simplex (dual feasible) or solved cold from
+                                the slack basis (neither).  Ignored for LPs
+                                with some b_i < 0. */
   int32_t device;          /* CUDA device ordinal; default 0 */
   int32_t use_graph;       /* 1 (default): replay plan launches as a CUDA graph */
   int32_t threads_per_cta; /* 0 = autotuned per size class */
@@ -115,6 +122,13 @@ typedef struct blpg_options {
                               step); 1: textbook minimum ratio.  Bland mode
                               always uses the textbook rule. */
   double feas_tol;         /* Harris relaxation; 0 = 1e-9 (FP64) / 1e-6 */
+  int32_t warm_mode;       /* a hinted basis that is primal- and dual-
+                              infeasible is finished by: 0 or 1 (default) a
+                              cost-shifted dual phase (negative reduced costs
+                              raised to small positive values, dual simplex
+                              to primal feasibility, true costs restored,
+                              primal simplex); 2 a cold solve from the slack
+                              basis */
 } blpg_options;
 
 /* Per-LP outputs (host memory for blpg_solve_batch, device memory for
@@ -127,7 +141,19 @@ typedef struct blpg_result {
   double* x;         /* nullable */
   int32_t* pivots;   /* nullable: simplex pivots performed per LP */
   int32_t* basis;    /* nullable: final basic column id of each row */
+  int32_t* info;     /* nullable: per-LP BLPG_INFO_* bits */
 } blpg_result;
+
+/* Bits of blpg_result.info. */
+enum {
+  BLPG_INFO_WARM = 1,     /* a basis hint was used */
+  BLPG_INFO_FALLBACK = 2, /* hinted basis primal- and dual-infeasible: cold solve */
+  BLPG_INFO_PARTIAL = 4,  /* some hinted columns found no pivot (singular) */
+  BLPG_INFO_DUAL = 8,     /* dual simplex pivots were taken */
+  BLPG_INFO_REFRESH = 16, /* FP64 refresh of the FP32 tableau ran */
+  BLPG_INFO_REPAIR = 32,  /* an FP64 check found a violation: more pivots */
+  BLPG_INFO_SHIFT = 64    /* hinted basis infeasible both ways: cost-shifted dual phase */
+};
 
 /* Fill *opt with the defaults above. */
 void blpg_options_init(blpg_options* opt);
@@ -207,6 +233,52 @@ int32_t blpg_solve_noalloc(int32_t count, int32_t max_m, int32_t max_n,
  * (the reference publishes no performance figures). */
 int32_t blpg_measure_peaks(int32_t device, double* smem_gbs, double* fp64_tflops,
                            double* fp32_tflops);
+
+/* ---------------------------------------------------------------------------
+ * Learned warm start (no reference counterpart): a multilayer perceptron that
+ * scores the n + m columns of an LP for membership in the optimal basis, from
+ * the LP's normalised [c; b; family one-hot].  BF16 tensor-core GEMMs with
+ * FP32 accumulation, FP32 master weights, Adam.  Dimensions are padded to
+ * multiples of 64 (blpg_mlp_dims); batches are multiples of 64 rows.  All
+ * data pointers are device pointers; X rows have width d_in_pad, label and
+ * logit rows width d_out_pad.
+ * ------------------------------------------------------------------------- */
+typedef struct blpg_mlp blpg_mlp;
+
+int32_t blpg_mlp_create(int32_t d_in, int32_t hidden, int32_t layers,
+                        int32_t d_out, int32_t max_batch, uint64_t seed,
+                        blpg_mlp** out);
+void blpg_mlp_destroy(blpg_mlp* mlp);
+int32_t blpg_mlp_dims(const blpg_mlp* mlp, int32_t* d_in_pad, int32_t* d_out_pad);
+int64_t blpg_mlp_num_params(const blpg_mlp* mlp);
+/* FP32 master parameters, packed W_1 b_1 ... W_L b_L (W_l: out_pad x in_pad). */
+int32_t blpg_mlp_get_params(const blpg_mlp* mlp, float* host_params);
+int32_t blpg_mlp_set_params(blpg_mlp* mlp, const float* host_params);
+/* One Adam step on a minibatch of B rows (labels 0/1); mean binary
+ * cross-entropy sum into *host_loss (nullable). */
+int32_t blpg_mlp_train_step(blpg_mlp* mlp, const float* dX, const float* dY,
+                            int32_t B, float lr, float* host_loss, void* stream);
+/* Logits of B rows (B a multiple of 64; larger than the training batch is
+ * fine, it is processed in chunks). */
+int32_t blpg_mlp_predict(blpg_mlp* mlp, const float* dX, int32_t B,
+                         float* dlogits, void* stream);
+/* Forward + backward without an update (gradient checks): packed gradients
+ * and the summed loss to host memory. */
+int32_t blpg_mlp_gradients(blpg_mlp* mlp, const float* dX, const float* dY,
+                           int32_t B, float* host_grads, float* host_loss);
+/* Features of `count` LPs with the same m, n: row k of dX (width ldx) is
+ * ((c_k, b_k) - mean[f]) / std[f] for the LP's family f = d_family[k]
+ * (mean/std: families x (n + m)), then the one-hot of f. */
+int32_t blpg_features(int32_t count, int32_t m, int32_t n, int32_t families,
+                      const int64_t* d_offb, const int64_t* d_offc,
+                      const double* db, const double* dc,
+                      const int32_t* d_family, const float* d_mean,
+                      const float* d_std, float* dX, int32_t ldx, void* stream);
+/* Basis hint from scores: for LP k, the m[k] highest-scoring of its
+ * n[k] + m[k] columns, in decreasing score order, at d_hint + d_offhint[k]. */
+int32_t blpg_topm_hint(const float* d_scores, int32_t lds, int32_t count,
+                       const int32_t* d_m, const int32_t* d_n, int32_t max_cols,
+                       const int64_t* d_offhint, int32_t* d_hint, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Reference batch files and synthetic workloads (host only, no GPU needed).

@@ -48,18 +48,21 @@ void oref_opts_init(oref_opts* o, int precision) {
   o->deg_tol = precision == OREF_FP32 ? 1e-7 : 1e-12;
   o->feas_tol = precision == OREF_FP32 ? 1e-6 : 1e-9;
   o->harris = 1;
+  o->ptol = precision == OREF_FP32 ? 1e-7 : 1e-9;
+  o->shift = 0.1;
+  o->composite = 1;
 }
 
 int oref_default_max_pivots(int m, int n) { return 50 * (m + n) + 1000; }
 
 int oref_solve_one(int m, int n, const double* A, const double* b,
-                   const double* c, const oref_opts* o_in, double* obj,
-                   double* x, int* basis, int* pivots) {
+                   const double* c, const oref_opts* o_in, const int* hint,
+                   double* obj, double* x, int* basis, int* pivots, int* info) {
   oref_opts o = *o_in;
   if (o.max_pivots <= 0) o.max_pivots = oref_default_max_pivots(m, n);
   if (o.precision == OREF_FP32)
-    return solve_one_f(m, n, A, b, c, &o, obj, x, basis, pivots);
-  return solve_one_d(m, n, A, b, c, &o, obj, x, basis, pivots);
+    return solve_one_f(m, n, A, b, c, &o, hint, obj, x, basis, pivots, info);
+  return solve_one_d(m, n, A, b, c, &o, hint, obj, x, basis, pivots, info);
 }
 
 typedef struct {
@@ -68,6 +71,8 @@ typedef struct {
   const int64_t *offA, *offb, *offc, *offx, *offbasis;
   const double *A, *b, *c;
   const oref_opts* o;
+  const int* hint;
+  int* info;
   int* status;
   double* obj;
   double* x;
@@ -86,10 +91,13 @@ static void* worker(void* arg) {
     if (k >= J->count) break;
     int piv = 0;
     double ob = 0.0;
+    int inf = 0;
     int st = oref_solve_one(J->m[k], J->n[k], J->A + J->offA[k], J->b + J->offb[k],
-                            J->c + J->offc[k], J->o, &ob,
+                            J->c + J->offc[k], J->o,
+                            J->hint ? J->hint + J->offbasis[k] : NULL, &ob,
                             J->x ? J->x + J->offx[k] : NULL,
-                            J->basis ? J->basis + J->offbasis[k] : NULL, &piv);
+                            J->basis ? J->basis + J->offbasis[k] : NULL, &piv, &inf);
+    if (J->info) J->info[k] = inf;
     J->status[k] = st;
     J->obj[k] = ob;
     if (J->pivots) J->pivots[k] = piv;
@@ -100,8 +108,8 @@ static void* worker(void* arg) {
 int oref_solve_batch(int count, const int* m, const int* n, const int64_t* offA,
                      const int64_t* offb, const int64_t* offc, const double* A,
                      const double* b, const double* c, const oref_opts* o,
-                     int threads, int* status, double* obj, double* x,
-                     int* pivots, int* basis) {
+                     int threads, const int* hint, int* status, double* obj,
+                     double* x, int* pivots, int* basis, int* info) {
   if (count < 0 || !m || !n || !A || !b || !c || !o || !status || !obj) return -1;
   int64_t* own = (int64_t*)malloc(sizeof(int64_t) * 5 * (size_t)(count + 1));
   if (!own) return -1;
@@ -133,6 +141,8 @@ int oref_solve_batch(int count, const int* m, const int* n, const int64_t* offA,
   J.x = x;
   J.pivots = pivots;
   J.basis = basis;
+  J.hint = hint;
+  J.info = info;
   pthread_mutex_init(&J.lock, NULL);
   if (threads < 1) threads = 1;
   if (threads > count) threads = count > 0 ? count : 1;

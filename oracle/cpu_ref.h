@@ -23,22 +23,27 @@ typedef struct {
   double deg_tol; /* a pivot with ratio <= deg_tol counts as degenerate */
   double feas_tol; /* Harris ratio-test relaxation */
   int harris;      /* 1: Harris two-pass ratio test outside Bland mode */
+  double ptol;     /* primal feasibility tolerance of the warm-start checks */
+  int composite;   /* 1: a hinted basis infeasible both ways is finished by a
+                      cost-shifted dual phase instead of a cold solve */
+  double shift;    /* size of the cost shift (the shifted d_j lie in [shift, 2 shift)) */
 } oref_opts;
 
 void oref_opts_init(oref_opts* o, int precision);
 int oref_default_max_pivots(int m, int n);
 
 int oref_solve_one(int m, int n, const double* A, const double* b,
-                   const double* c, const oref_opts* o, double* obj, double* x,
-                   int* basis, int* pivots);
+                   const double* c, const oref_opts* o, const int* hint,
+                   double* obj, double* x, int* basis, int* pivots, int* info);
 
-/* Null offsets = packed.  x (nullable) follows off_c; basis (nullable) is
- * packed m per LP.  threads = POSIX threads across LPs. */
+/* Null offsets = packed.  x (nullable) follows off_c; basis and hint
+ * (nullable) are packed m per LP; info (nullable) gets the warm-start bits
+ * (1 warm, 2 fallback, 4 partial, 8 dual).  threads = POSIX threads. */
 int oref_solve_batch(int count, const int* m, const int* n, const int64_t* offA,
                      const int64_t* offb, const int64_t* offc, const double* A,
                      const double* b, const double* c, const oref_opts* o,
-                     int threads, int* status, double* obj, double* x,
-                     int* pivots, int* basis);
+                     int threads, const int* hint, int* status, double* obj,
+                     double* x, int* pivots, int* basis, int* info);
 
 #ifdef __cplusplus
 }

@@ -154,11 +154,142 @@ static int FN(simplex_loop)(FN(tab_t) * t, int ncols, const oref_opts* o,
   }
 }
 
+/* Objective row from the current basis: d_j = sum_i cB_i T_ij - c_j,
+ * z = sum_i cB_i rhs_i (sums over rows in increasing order). */
+static void FN(objective_row)(FN(tab_t) * t, const double* c) {
+  const int m = t->m, n = t->n, rhs = t->W - 1;
+  for (int j = 0; j < t->W; ++j) {
+    REAL acc = (REAL)0;
+    for (int i = 0; i < m; ++i) {
+      const int bi = t->basis[i];
+      const REAL cb = bi < n ? (REAL)c[bi] : (REAL)0;
+      acc = FMA(cb, TT(t, i, j), acc);
+    }
+    const REAL cj = j < n ? (REAL)c[j] : (REAL)0;
+    TT(t, m, j) = j == rhs ? acc : acc - cj;
+  }
+}
+
+/* Feasibility of the tableau: bit 0 when every RHS >= -ptol, bit 1 when
+ * every reduced cost d_j (j < n+m) >= -opt_tol (the GPU's check_feasible). */
+static int FN(check)(const FN(tab_t) * t, REAL ptol, REAL opt_tol) {
+  int ok = 3;
+  for (int i = 0; i < t->m; ++i)
+    if (TT(t, i, t->W - 1) < -ptol) ok &= ~1;
+  for (int j = 0; j < t->n + t->m; ++j)
+    if (TT(t, t->m, j) < -opt_tol) ok &= ~2;
+  return ok;
+}
+
+/* Dual simplex from a dual-feasible basis: leaving row = most negative RHS
+ * below -ptol (ties lowest basic variable), entering column = minimum
+ * max(d_j, 0) / -T_rj over T_rj < -piv_tol (ties lowest column). */
+static int FN(dual_loop)(FN(tab_t) * t, const oref_opts* o, int* pivots, REAL* f, REAL ptol) {
+  const REAL piv_tol = (REAL)o->piv_tol;
+  const int m = t->m, ncols = t->n + t->m;
+  for (;;) {
+    int r = -1, rb = 0;
+    REAL best = (REAL)0;
+    for (int i = 0; i < m; ++i) {
+      const REAL v = TT(t, i, t->W - 1);
+      if (!(v < -ptol)) continue;
+      if (r < 0 || v < best || (v == best && t->basis[i] < rb)) {
+        r = i;
+        best = v;
+        rb = t->basis[i];
+      }
+    }
+    if (r < 0) return OREF_OPT;
+    if (*pivots >= o->max_pivots) return OREF_UNDEF;
+    int q = -1;
+    if (!o->harris) {
+      REAL bth = (REAL)0;
+      for (int j = 0; j < ncols; ++j) {
+        const REAL a = TT(t, r, j);
+        if (!(a < -piv_tol)) continue;
+        const REAL dj = TT(t, m, j);
+        const REAL th = dj > (REAL)0 ? dj / (-a) : (REAL)0;
+        if (q < 0 || th < bth) {
+          q = j;
+          bth = th;
+        }
+      }
+    } else {
+      /* Harris: bound by ratios relaxed by opt_tol, then the largest |T_rj| */
+      REAL tmax = (REAL)0;
+      int any = 0;
+      for (int j = 0; j < ncols; ++j) {
+        const REAL a = TT(t, r, j);
+        if (!(a < -piv_tol)) continue;
+        const REAL dj = TT(t, m, j);
+        const REAL th = ((dj > (REAL)0 ? dj : (REAL)0) + (REAL)o->opt_tol) / (-a);
+        if (!any || th < tmax) tmax = th;
+        any = 1;
+      }
+      REAL amax = (REAL)0;
+      for (int j = 0; any && j < ncols; ++j) {
+        const REAL a = TT(t, r, j);
+        if (!(a < -piv_tol)) continue;
+        const REAL dj = TT(t, m, j);
+        const REAL th = dj > (REAL)0 ? dj / (-a) : (REAL)0;
+        if (th <= tmax && (q < 0 || -a > amax)) {
+          q = j;
+          amax = -a;
+        }
+      }
+    }
+    if (q < 0) return OREF_NOFEAS;
+    FN(pivot)(t, r, q, f);
+    *pivots += 1;
+  }
+}
+
+/* Warm start: pivot each hinted structural column into the basis on the
+ * row, among rows whose basic variable is a slack the hint does not keep,
+ * with the largest |T_ij| (ties lowest row).  Returns how many hinted
+ * columns found no pivot. */
+static int FN(crash)(FN(tab_t) * t, const int* hint, const oref_opts* o, int* pivots, REAL* f) {
+  const int m = t->m, n = t->n;
+  const REAL piv_tol = (REAL)o->piv_tol;
+  int* keep = (int*)calloc((size_t)(m > 0 ? m : 1), sizeof(int));
+  for (int k = 0; k < m; ++k)
+    if (hint[k] >= n && hint[k] < n + m) keep[hint[k] - n] = 1;
+  int missing = 0;
+  for (int k = 0; k < m; ++k) {
+    const int h = hint[k];
+    if (h < 0 || h >= n) continue;
+    int isbasic = 0;
+    for (int i = 0; i < m; ++i) isbasic |= t->basis[i] == h;
+    if (isbasic) continue;
+    int r = -1;
+    REAL best = (REAL)0;
+    for (int i = 0; i < m; ++i) {
+      const int bi = t->basis[i];
+      if (bi < n || bi >= n + m || keep[bi - n]) continue;
+      const REAL v = TT(t, i, h);
+      const REAL av = v < (REAL)0 ? -v : v;
+      if (av > piv_tol && (r < 0 || av > best)) {
+        r = i;
+        best = av;
+      }
+    }
+    if (r < 0) {
+      ++missing;
+      continue;
+    }
+    FN(pivot)(t, r, h, f);
+    *pivots += 1;
+  }
+  free(keep);
+  return missing;
+}
+
 /* Solve one LP.  Returns the status; fills objective, x (n, nullable),
  * basis (m, nullable), pivot count. */
 static int FN(solve_one)(int m, int n, const double* A, const double* b,
-                         const double* c, const oref_opts* o, double* obj,
-                         double* x, int* basis_out, int* pivots_out) {
+                         const double* c, const oref_opts* o, const int* hint,
+                         double* obj, double* x, int* basis_out, int* pivots_out,
+                         int* info_out) {
   int na = 0;
   for (int i = 0; i < m; ++i)
     if (b[i] < 0) ++na;
@@ -177,8 +308,14 @@ static int FN(solve_one)(int m, int n, const double* A, const double* b,
     return -1;
   }
   const int rhs = t.W - 1;
+  int info = 0;
+  int pivots = 0, bland = 0, degen = 0, st;
+reload:;
+  bland = 0; /* a cold reload restarts the rule state; pivots keep counting */
+  degen = 0;
   /* slack-basis tableau (simplex.cu:506-534); rows with b_i < 0 are negated
    * and get an artificial column (simplex.cu:642-686). */
+  memset(t.T, 0, sizeof(REAL) * (size_t)(m + 1) * t.W);
   int k = 0;
   for (int i = 0; i < m; ++i) {
     const REAL sgn = b[i] < 0 ? (REAL)-1 : (REAL)1;
@@ -196,7 +333,6 @@ static int FN(solve_one)(int m, int n, const double* A, const double* b,
       t.basis[i] = n + i;
     }
   }
-  int pivots = 0, bland = 0, degen = 0, st;
   if (na > 0) {
     /* phase I: maximise -sum(artificials); row m = -sum of artificial rows */
     for (int j = 0; j < t.W; ++j) {
@@ -227,23 +363,45 @@ static int FN(solve_one)(int m, int n, const double* A, const double* b,
         }
       }
       /* phase II objective row: d_j = sum_i cB_i T_ij - c_j, z = sum cB_i rhs_i */
-      for (int j = 0; j < t.W; ++j) {
-        REAL acc = (REAL)0;
-        for (int i = 0; i < m; ++i) {
-          const int bi = t.basis[i];
-          const REAL cb = bi < n ? (REAL)c[bi] : (REAL)0;
-          acc = FMA(cb, TT(&t, i, j), acc);
-        }
-        const REAL cj = j < n ? (REAL)c[j] : (REAL)0;
-        TT(&t, m, j) = j == rhs ? acc : acc - cj;
-      }
+      FN(objective_row)(&t, c);
       bland = 0;
       degen = 0;
       st = FN(simplex_loop)(&t, n + m, o, &pivots, &bland, &degen, f);
     }
   } else {
     for (int j = 0; j < n; ++j) TT(&t, m, j) = -(REAL)c[j];
-    st = FN(simplex_loop)(&t, n + m, o, &pivots, &bland, &degen, f);
+    st = -1;
+    if (hint && !(info & 2)) {
+      const REAL ptol = (REAL)o->ptol, opt_tol = (REAL)o->opt_tol;
+      info |= 1;
+      if (FN(crash)(&t, hint, o, &pivots, f) > 0) info |= 4;
+      const int fl = FN(check)(&t, ptol, opt_tol);
+      if (fl & 1) {
+        st = FN(simplex_loop)(&t, n + m, o, &pivots, &bland, &degen, f);
+      } else if (fl & 2) {
+        info |= 8;
+        st = FN(dual_loop)(&t, o, &pivots, f, ptol);
+        if (st == OREF_OPT) st = FN(simplex_loop)(&t, n + m, o, &pivots, &bland, &degen, f);
+      } else if (o->composite) {
+        /* infeasible both ways: shift the costs of the columns with
+         * d_j < -opt_tol to make d_j = 0 (dual feasible), dual simplex to a
+         * primal-feasible basis, restore the true costs, primal simplex */
+        info |= 8 | 64;
+        for (int j = 0; j < n + m; ++j)
+          if (TT(&t, m, j) < -opt_tol)
+            TT(&t, m, j) = (REAL)o->shift * ((REAL)1 + (REAL)((j * 7919) % 1000) / (REAL)1000);
+        st = FN(dual_loop)(&t, o, &pivots, f, ptol);
+        if (st == OREF_OPT) {
+          FN(objective_row)(&t, c);
+          st = FN(simplex_loop)(&t, n + m, o, &pivots, &bland, &degen, f);
+        }
+      }
+      if (st < 0 || st == OREF_NOFEAS) {
+        info |= 2; /* infeasible both ways: cold solve from the slack basis */
+        goto reload;
+      }
+    }
+    if (st < 0) st = FN(simplex_loop)(&t, n + m, o, &pivots, &bland, &degen, f);
   }
   *obj = (double)TT(&t, m, rhs);
   if (x) {
@@ -254,6 +412,7 @@ static int FN(solve_one)(int m, int n, const double* A, const double* b,
   if (basis_out)
     for (int i = 0; i < m; ++i) basis_out[i] = t.basis[i];
   *pivots_out = pivots;
+  if (info_out) *info_out = info;
   free(t.T);
   free(t.basis);
   free(f);

@@ -23,7 +23,8 @@ class Opts(C.Structure):
         ("precision", C.c_int), ("max_pivots", C.c_int), ("bland_after", C.c_int),
         ("refactor_period", C.c_int), ("opt_tol", C.c_double), ("piv_tol", C.c_double),
         ("phase1_tol", C.c_double), ("deg_tol", C.c_double), ("feas_tol", C.c_double),
-        ("harris", C.c_int),
+        ("harris", C.c_int), ("ptol", C.c_double), ("composite", C.c_int),
+        ("shift", C.c_double),
     ]
 
 
@@ -40,9 +41,10 @@ def lib():
         L.oref_opts_init.restype = None
         ip, lp, dp = C.POINTER(C.c_int), C.POINTER(C.c_int64), C.POINTER(C.c_double)
         L.oref_solve_batch.argtypes = [C.c_int, ip, ip, lp, lp, lp, dp, dp, dp, C.POINTER(Opts),
-                                       C.c_int, ip, dp, dp, ip, ip]
+                                       C.c_int, ip, ip, dp, dp, ip, ip, ip]
         L.oref_solve_batch.restype = C.c_int
-        L.oref_solve_one.argtypes = [C.c_int, C.c_int, dp, dp, dp, C.POINTER(Opts), dp, dp, ip, ip]
+        L.oref_solve_one.argtypes = [C.c_int, C.c_int, dp, dp, dp, C.POINTER(Opts), ip, dp, dp, ip,
+                                     ip, ip]
         L.oref_solve_one.restype = C.c_int
         _lib = L
     return _lib
@@ -63,6 +65,7 @@ class RefResult:
     pivots: np.ndarray
     x: Optional[np.ndarray] = None
     basis: Optional[np.ndarray] = None
+    info: Optional[np.ndarray] = None
 
 
 def _p(a, t):
@@ -70,7 +73,7 @@ def _p(a, t):
 
 
 def solve_batch(batch, precision: str = "fp64", threads: Optional[int] = None, want_x=False,
-                want_basis=False, **kw) -> RefResult:
+                want_basis=False, hint=None, **kw) -> RefResult:
     """Solve a simplexprojects_gb300.LPBatch on the CPU with the oracle."""
     L = lib()
     k = batch.count
@@ -82,14 +85,18 @@ def solve_batch(batch, precision: str = "fp64", threads: Optional[int] = None, w
     pv = np.zeros(k, np.int32)
     x = np.zeros(int((oc + n).max()) if k else 0) if want_x else None
     bs = np.zeros(int(m.sum()), np.int32) if want_basis else None
+    info = np.zeros(k, np.int32)
+    if hint is not None:
+        hint = np.ascontiguousarray(hint, dtype=np.int32)
+        assert hint.size == int(m.sum())
     o = opts(precision, **kw)
     if threads is None:
         threads = os.cpu_count() or 1
     rc = L.oref_solve_batch(k, _p(m, C.c_int), _p(n, C.c_int), _p(oA, C.c_int64),
                             _p(ob, C.c_int64), _p(oc, C.c_int64), _p(batch.A, C.c_double),
                             _p(batch.b, C.c_double), _p(batch.c, C.c_double), C.byref(o),
-                            int(threads), _p(st, C.c_int), _p(obj, C.c_double), _p(x, C.c_double),
-                            _p(pv, C.c_int), _p(bs, C.c_int))
+                            int(threads), _p(hint, C.c_int), _p(st, C.c_int), _p(obj, C.c_double),
+                            _p(x, C.c_double), _p(pv, C.c_int), _p(bs, C.c_int), _p(info, C.c_int))
     if rc != 0:
         raise RuntimeError("oref_solve_batch failed")
-    return RefResult(st, obj, pv, x, bs)
+    return RefResult(st, obj, pv, x, bs, info)

@@ -39,12 +39,14 @@ class Options(C.Structure):
         ("basis_hint", i32p), ("device", C.c_int32), ("use_graph", C.c_int32),
         ("threads_per_cta", C.c_int32), ("max_cluster", C.c_int32), ("min_cluster", C.c_int32),
         ("cta_smem_budget", C.c_int32), ("ratio_rule", C.c_int32), ("feas_tol", C.c_double),
+        ("warm_mode", C.c_int32),
     ]
 
 
 class Result(C.Structure):
     _fields_ = [
         ("status", i32p), ("objective", f64p), ("x", f64p), ("pivots", i32p), ("basis", i32p),
+        ("info", i32p),
     ]
 
 
@@ -65,6 +67,21 @@ SIGNATURES = {
     "blpg_measure_peaks": (C.c_int32, [C.c_int32, f64p, f64p, f64p]),
     "blpg_solve_noalloc": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32] + [C.c_void_p] * 8
                            + [C.c_int32] + [C.c_void_p] * 5),
+    "blpg_mlp_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                    C.c_uint64, C.POINTER(C.c_void_p)]),
+    "blpg_mlp_destroy": (None, [C.c_void_p]),
+    "blpg_mlp_dims": (C.c_int32, [C.c_void_p, i32p, i32p]),
+    "blpg_mlp_num_params": (C.c_int64, [C.c_void_p]),
+    "blpg_mlp_get_params": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float)]),
+    "blpg_mlp_set_params": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float)]),
+    "blpg_mlp_train_step": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_float,
+                                        C.POINTER(C.c_float), C.c_void_p]),
+    "blpg_mlp_predict": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "blpg_mlp_gradients": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                       C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "blpg_features": (C.c_int32, [C.c_int32] * 4 + [C.c_void_p] * 8 + [C.c_int32, C.c_void_p]),
+    "blpg_topm_hint": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                   C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "blpg_read_abc": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, i32p, i32p, f64p, f64p, f64p]),
     "blpg_gen_shapes": (C.c_int64, [C.c_int32, C.c_int64, C.c_int32, C.c_uint64, i32p, i32p, i32p]),
     "blpg_gen_fill": (C.c_int32, [C.c_int32, C.c_int64, C.c_int32, C.c_uint64, i32p, i32p, f64p,

@@ -46,6 +46,7 @@ SOURCES = [
     ("blpg_api.cu", ["--fmad=false"]),
     ("blpg_peaks.cu", []),
     ("blpg_noalloc.cu", ["--fmad=false"]),
+    ("blpg_mlp.cu", []),
     ("blpg_gen.cpp", []),
 ]
 
@@ -95,6 +96,29 @@ def build_library(verbose: bool = False) -> Path:
     return LIB
 
 
+CLI = LIBDIR / "blpg_cli"
+
+
+def build_cli(verbose: bool = False) -> Path:
+    """The reference-compatible command line (csrc/blpg_cli.cpp), linked
+    against libblpg.so with an $ORIGIN rpath."""
+    nvcc = _nvcc()
+    src = CSRC / "blpg_cli.cpp"
+    deps = [src, ROOT / "include" / "blpg.h", ROOT / "include" / "blpg_simplex.hpp", LIB]
+    if CLI.exists() and CLI.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return CLI
+    tmp = CLI.with_name("blpg_cli.tmp")
+    cmd = [nvcc, "-std=c++17", "-O2", "-x", "c++", str(src), "-I", str(ROOT / "include"),
+           "-L", str(LIBDIR), "-lblpg", "-Xlinker", "-rpath,$ORIGIN", "-o", str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"cli build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CLI)
+    if verbose:
+        print(f"built {CLI}")
+    return CLI
+
+
 def build_oracle(verbose: bool = False) -> Path:
     ORACLE_BUILD.mkdir(exist_ok=True)
     srcs = [ORACLE_DIR / "cpu_ref.c"]
@@ -120,6 +144,7 @@ def build_all(verbose: bool = False) -> None:
         f2 = ex.submit(build_oracle, verbose)
         f1.result()
         f2.result()
+    build_cli(verbose)
 
 
 if __name__ == "__main__":

@@ -535,7 +535,6 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
 extern "C" int32_t blpg_plan_execute(blpg_plan* p, const double* dA, const double* db,
                                      const double* dc, const int32_t* basis_hint,
                                      blpg_result* out, void* stream_v) {
-  (void)basis_hint;
   if (!p || !out || !out->status || !out->objective)
     return fail(BLPG_EINVAL, "blpg_plan_execute: null plan or outputs");
   if (p->count == 0) return BLPG_OK;
@@ -566,6 +565,12 @@ extern "C" int32_t blpg_plan_execute(blpg_plan* p, const double* dA, const doubl
   a.phase1_tol = fp32 ? 1e-4 : 1e-7;
   a.deg_tol = fp32 ? 1e-7 : 1e-12;
   a.harris = p->opt.ratio_rule == 1 ? 0 : 1;
+  a.ptol = fp32 ? 1e-7 : 1e-9;
+  a.refresh_period = p->opt.refactor_period > 0 ? p->opt.refactor_period : 0;
+  a.hint = basis_hint;
+  a.info = out->info;
+  a.warm_mode = p->opt.warm_mode == 0 ? 1 : (p->opt.warm_mode == 2 ? 0 : 1);
+  a.shift = 0.1;
   a.max_pivots = p->opt.max_pivots;
   a.bland_after = p->opt.bland_after > 0 ? p->opt.bland_after : 64;
   CK(cudaEventRecord(p->ev_in, user));
@@ -652,7 +657,10 @@ static Workspace g_ws;
 static bool plan_matches(const Workspace& w, const blpg_batch* bt, const blpg_options& o,
                          const std::vector<int32_t>& shapes,
                          const std::vector<int64_t>& offs) {
-  return w.plan && std::memcmp(&w.key_opt, &o, sizeof(o)) == 0 && w.key_shapes == shapes &&
+  blpg_options a = w.key_opt, b = o;
+  a.basis_hint = nullptr;
+  b.basis_hint = nullptr;
+  return w.plan && std::memcmp(&a, &b, sizeof(a)) == 0 && w.key_shapes == shapes &&
          w.key_offs == offs && w.plan->count == bt->count;
 }
 }  // namespace blpg
@@ -711,8 +719,10 @@ extern "C" int32_t blpg_solve_batch(const blpg_batch* bt, const blpg_options* op
                sc = al(sizeof(double) * p->extc), sst = al(sizeof(int32_t) * N),
                sob = al(sizeof(double) * N), sx = al(sizeof(double) * p->extx),
                spv = al(sizeof(int32_t) * N), sbs = al(sizeof(int32_t) * p->extbasis);
+  const bool hint = opt.basis_hint != nullptr;
   const size_t need = sA + sb + sc + sst + sob + (out->x ? sx : 0) +
-                      (out->pivots ? spv : 0) + (out->basis ? sbs : 0);
+                      (out->pivots ? spv : 0) + (out->basis ? sbs : 0) +
+                      (out->info ? spv : 0) + (hint ? sbs : 0);
   if (g_ws.cap < need || g_ws.device != p->device) {
     if (g_ws.buf) cudaFree(g_ws.buf);
     g_ws.buf = nullptr;
@@ -743,11 +753,23 @@ extern "C" int32_t blpg_solve_batch(const blpg_batch* bt, const blpg_options* op
     dres.basis = (int32_t*)o;
     o += sbs;
   }
+  if (out->info) {
+    dres.info = (int32_t*)o;
+    o += spv;
+  }
+  int32_t* dhint = nullptr;
+  if (hint) {
+    dhint = (int32_t*)o;
+    o += sbs;
+  }
   cudaStream_t s = p->stream;
+  if (hint)
+    CK(cudaMemcpyAsync(dhint, opt.basis_hint, sizeof(int32_t) * p->extbasis,
+                       cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(dA, bt->A, sizeof(double) * p->extA, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(db, bt->b, sizeof(double) * p->extb, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(dc, bt->c, sizeof(double) * p->extc, cudaMemcpyHostToDevice, s));
-  if ((rc = blpg_plan_execute(p, dA, db, dc, nullptr, &dres, s))) return rc;
+  if ((rc = blpg_plan_execute(p, dA, db, dc, dhint, &dres, s))) return rc;
   CK(cudaMemcpyAsync(out->status, dres.status, sizeof(int32_t) * N, cudaMemcpyDeviceToHost,
                      s));
   CK(cudaMemcpyAsync(out->objective, dres.objective, sizeof(double) * N,
@@ -760,6 +782,8 @@ extern "C" int32_t blpg_solve_batch(const blpg_batch* bt, const blpg_options* op
   if (out->basis)
     CK(cudaMemcpyAsync(out->basis, dres.basis, sizeof(int32_t) * p->extbasis,
                        cudaMemcpyDeviceToHost, s));
+  if (out->info)
+    CK(cudaMemcpyAsync(out->info, dres.info, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   CK(cudaGetLastError());
   return BLPG_OK;

@@ -210,6 +210,12 @@ extern "C" int32_t blpg_solve_noalloc(int32_t count, int32_t max_m, int32_t max_
   a.harris = 1;
   a.max_pivots = 0;
   a.bland_after = 64;
+  a.hint = nullptr;
+  a.info = nullptr;
+  a.ptol = fp32 ? 1e-7 : 1e-9;
+  a.refresh_period = 0;
+  a.warm_mode = 1;
+  a.shift = 0.1;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   return fp32 ? run<float>(count, max_m, max_n, a, st.scratch, prop, s)
               : run<double>(count, max_m, max_n, a, st.scratch, prop, s);

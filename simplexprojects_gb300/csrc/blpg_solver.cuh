@@ -63,7 +63,22 @@ struct LpArgs {
   int32_t harris;   // 1: Harris two-pass ratio test outside Bland mode
   int32_t max_pivots;  // <= 0: 50 (m + n) + 1000
   int32_t bland_after;
+  const int32_t* hint;  // nullable: m basic column ids per LP (offbasis layout)
+  int32_t* info;        // nullable: per-LP flags (kInfo*)
+  double ptol;          // primal feasibility tolerance of the final checks
+  int32_t refresh_period;  // FP32: FP64 refresh every k pivots (0: at the end)
+  int32_t warm_mode;       // 0: hinted basis infeasible both ways -> cold; 1: cost-shifted dual
+  double shift;            // cost shift of warm_mode 1
 };
+
+// Bits of the per-LP info output.
+constexpr int kInfoWarm = 1;       // a basis hint was used
+constexpr int kInfoFallback = 2;   // hinted basis infeasible both ways: cold solve
+constexpr int kInfoPartial = 4;    // some hinted columns found no pivot
+constexpr int kInfoDual = 8;       // dual simplex pivots were taken
+constexpr int kInfoRefresh = 16;   // FP64 refresh of the FP32 tableau ran
+constexpr int kInfoRepair = 32;    // a refresh found a violation (more pivots)
+constexpr int kInfoShift = 64;     // hinted basis infeasible both ways: cost-shifted dual phase
 
 struct ClassArgs {
   const int32_t* order;  // LP ids of this class, heaviest first
@@ -110,7 +125,7 @@ struct Geom {
 
 // Shared-memory layout of a class (bytes).  Identical on host and device.
 struct Layout {
-  int tab, colA, colB, rhsx, basis, red, state, total;
+  int tab, colA, colB, rhsx, basis, flags, ext, red, state, total;
   __host__ __device__ Layout(int max_m, int max_ldw, int elem) {
     int mp1 = round_up(max_m + 1, 4);
     tab = 0;
@@ -123,10 +138,14 @@ struct Layout {
     off += round_up(mp1 * elem, 16);
     basis = off;
     off += round_up(mp1 * 4, 16);
+    flags = off;
+    off += round_up(mp1 * 4, 16);
+    ext = off;
+    if (elem == 4) off += 2 * mp1 * 8;  // FP64 x_B and duals of the refresh
     red = off;
     off += 3 * 32 * 16;  // three argmin scratch buffers (pricing, ratio, Harris)
     state = off;
-    off += 64;
+    off += 80;
     total = off;
   }
 };
@@ -196,6 +215,14 @@ __device__ __forceinline__ Key ratio_key(double th, int bid, int row) {
 __device__ __forceinline__ Key ratio_key(float th, int bid, int row) {
   return Key{__float_as_uint(th), 0u, (unsigned)bid, (unsigned)row};
 }
+// Most negative value first (as price_key), ties by `tie`, payload `row`.
+__device__ __forceinline__ Key neg_key(double v, int tie, int row) {
+  unsigned long long u = ~(unsigned long long)__double_as_longlong(v);
+  return Key{(unsigned)(u >> 32), (unsigned)u, (unsigned)tie, (unsigned)row};
+}
+__device__ __forceinline__ Key neg_key(float v, int tie, int row) {
+  return Key{~__float_as_uint(v), 0u, (unsigned)tie, (unsigned)row};
+}
 // Largest positive value first: ~bits is decreasing in a positive value.
 __device__ __forceinline__ Key big_key(double a, int bid, int row) {
   unsigned long long u = ~(unsigned long long)__double_as_longlong(a);
@@ -239,6 +266,7 @@ __device__ __forceinline__ float4 v_div(const float4& a, float d) {
 
 // Status codes (GLPK numbering, as blpg.h)
 constexpr int kUndef = 1, kNoFeas = 4, kOpt = 5, kUnbnd = 6;
+constexpr int kRefresh = 100;  // internal: the primal loop paused for a refresh
 
 struct SharedState {
   int ticket;
@@ -247,6 +275,7 @@ struct SharedState {
   double theta;
   Key pslot;
   Key aux;
+  double z;  // FP64 objective of the last refresh
 };
 
 // ---------------------------------------------------------------------------
@@ -265,6 +294,9 @@ struct Solver {
   __device__ T* colbuf(int k) const { return k ? col1 : col0; }
   T* rhsx;
   int* basis;
+  int* flags;
+  double* xr;  // FP32 tableau only: FP64 x_B of the refresh
+  double* yr;  // FP32 tableau only: FP64 duals of the refresh
   Key* redP;
   Key* redR;
   Key* redH;
@@ -447,7 +479,8 @@ struct Solver {
   // The primal simplex loop from the current tableau (the oracle's
   // simplex_loop).  Pricing covers global columns [0, price_cols).
   __device__ int loop(const Geom& g, int c0, int lc, int price_cols, const LpArgs& a,
-                      int max_piv, int& pivots, bool& bland, int& degen, int& cur) {
+                      int max_piv, int& pivots, bool& bland, int& degen, int& cur,
+                      int period = 0) {
     const T opt_tol = (T)a.opt_tol, piv_tol = (T)a.piv_tol, feas_tol = (T)a.feas_tol;
     const T deg_tol = (T)a.deg_tol;
     Key kq = price_only(g, c0, lc, bland, opt_tol, price_cols);
@@ -501,6 +534,7 @@ struct Solver {
       ++pivots;
       if (qn < 0) return kOpt;
       if (pivots >= max_piv) return kUndef;
+      if (period > 0 && pivots % period == 0) return kRefresh;
       q = qn;
       owner = owner_n;
     }
@@ -559,30 +593,363 @@ struct Solver {
       k = cluster_min(k);
       if (CLUSTER) csync();  // pslot reads done before the next write
       if (k.w2 == ~0u) continue;  // redundant row: artificial stays basic at 0
-      const int q = (int)k.w2;
-      const int owner = q / g.cw;
-      if (owner == rank) extract(g, q, c0, colbuf(cur));
-      if (CLUSTER) {
-        csync();
-        if (owner != rank) {
-          const T* src = remote(colbuf(cur), owner);
-          for (int e = threadIdx.x; e <= g.m; e += blockDim.x) colbuf(cur)[e] = src[e];
-        }
-      }
-      __syncthreads();
-      const T* pcol = colbuf(cur);
-      // pivot without pricing: reuse pivot_rows with an impossible tolerance
-      pivot_rows(g, i, pcol, c0, lc, false, T(0), 0);
-      if (threadIdx.x == 0) basis[i] = q;
-      update_body(g, i, pcol, -1, -1, c0, colbuf(cur ^ 1));
-      __syncthreads();
-      if (CLUSTER) csync();  // column copies done before the owner's next extract
+      pivot_on(g, i, (int)k.w2, c0, lc, cur);
       ++pivots;
     }
   }
 
+  // Pivot on (r, q) without pricing (phase-I drive-out, warm-start crash,
+  // dual simplex).  Column q is extracted by its owner and copied by the
+  // other CTAs of the cluster; returns with every copy done.
+  __device__ void pivot_on(const Geom& g, int r, int q, int c0, int lc, int cur) {
+    const int owner = q / g.cw;
+    if (owner == rank) extract(g, q, c0, colbuf(cur));
+    if (CLUSTER) {
+      csync();
+      if (owner != rank) {
+        const T* src = remote(colbuf(cur), owner);
+        for (int e = threadIdx.x; e <= g.m; e += blockDim.x) colbuf(cur)[e] = src[e];
+      }
+    }
+    __syncthreads();
+    const T* pcol = colbuf(cur);
+    pivot_rows(g, r, pcol, c0, lc, false, T(0), 0);
+    if (threadIdx.x == 0) basis[r] = q;
+    update_body(g, r, pcol, -1, -1, c0, colbuf(cur ^ 1));
+    __syncthreads();
+    if (CLUSTER) csync();
+  }
+
+  // Cluster-wide OR of a block-level flag.
+  __device__ bool cluster_any(bool v) {
+    v = __syncthreads_or(v ? 1 : 0) != 0;
+    if (!CLUSTER) return v;
+    if (threadIdx.x == 0) sh->aux.w0 = v ? 1u : 0u;
+    csync();
+    bool any = false;
+    for (int k = 0; k < K; ++k) any = any || remote(&sh->aux, k)->w0 != 0u;
+    csync();
+    return any;
+  }
+
+  // Feasibility of the current tableau: bit 0 when every x_B >= -ptol,
+  // bit 1 when every reduced cost d_j (j < n+m) >= -opt_tol.
+  __device__ int check_feasible(const Geom& g, int c0, int lc, T ptol, T opt_tol) {
+    bool badp = false, badd = false;
+    for (int i = threadIdx.x; i < g.m; i += blockDim.x)
+      badp = badp || tab[(size_t)i * g.ldw + g.cw] < -ptol;
+    const T* d = tab + (size_t)g.m * g.ldw;
+    for (int lj = threadIdx.x; lj < lc; lj += blockDim.x)
+      badd = badd || (c0 + lj < g.n + g.m && d[lj] < -opt_tol);
+    badp = __syncthreads_or(badp ? 1 : 0) != 0;  // RHS is replicated: no exchange
+    badd = cluster_any(badd);
+    return (badp ? 0 : 1) | (badd ? 0 : 2);
+  }
+
+  // Dual simplex from a dual-feasible basis (the oracle's dual_loop):
+  // leaving row = most negative RHS below -ptol (ties lowest basic
+  // variable); entering column = minimum max(d_j, 0) / -T_rj over
+  // T_rj < -piv_tol (ties lowest column).  kOpt once x_B >= -ptol; kNoFeas
+  // when no column can enter (the LP would be primal infeasible).
+  __device__ int dual_loop(const Geom& g, int c0, int lc, const LpArgs& a, int max_piv,
+                           int& pivots, int cur, T ptol) {
+    const T piv_tol = (T)a.piv_tol;
+    for (;;) {
+      Key kr = key_none();
+      for (int i = threadIdx.x; i < g.m; i += blockDim.x) {
+        const T v = tab[(size_t)i * g.ldw + g.cw];
+        if (v < -ptol) {
+          Key kk = neg_key(v, basis[i], i);
+          if (key_less(kk, kr)) kr = kk;
+        }
+      }
+      kr = block_min(kr, redR);  // RHS replicated: every CTA finds the same row
+      if (kr.w2 == ~0u) return kOpt;
+      if (pivots >= max_piv) return kUndef;
+      const int r = (int)kr.w3;
+      const T* row = tab + (size_t)r * g.ldw;
+      const T* drow = tab + (size_t)g.m * g.ldw;
+      const T dual_tol = (T)a.opt_tol;
+      // Harris (as the primal test): pass 1 bounds the dual step by the
+      // ratios relaxed by opt_tol, pass 2 takes the largest |T_rj| within it
+      // (ties lowest column).  Textbook rule when Harris is off.
+      Key kq = key_none();
+      for (int lj = threadIdx.x; lj < lc; lj += blockDim.x) {
+        const int j = c0 + lj;
+        const T arj = row[lj];
+        if (j < g.n + g.m && arj < -piv_tol) {
+          const T dj = drow[lj];
+          const T th = a.harris ? ((dj > T(0) ? dj : T(0)) + dual_tol) / (-arj)
+                                : (dj > T(0) ? dj / (-arj) : T(0));
+          Key kk = ratio_key(th, j, 0);
+          if (key_less(kk, kq)) kq = kk;
+        }
+      }
+      kq = block_min(kq, redH);
+      kq = cluster_min(kq);
+      if (CLUSTER) csync();  // pslot reads done before the next cluster_min
+      if (kq.w2 == ~0u) return kNoFeas;
+      if (a.harris) {
+        const T tmax = key_theta(kq, T(0));
+        Key k2 = key_none();
+        for (int lj = threadIdx.x; lj < lc; lj += blockDim.x) {
+          const int j = c0 + lj;
+          const T arj = row[lj];
+          if (j < g.n + g.m && arj < -piv_tol) {
+            const T dj = drow[lj];
+            const T th = dj > T(0) ? dj / (-arj) : T(0);
+            if (th <= tmax) {
+              Key kk = big_key(-arj, j, 0);
+              if (key_less(kk, k2)) k2 = kk;
+            }
+          }
+        }
+        k2 = block_min(k2, redP);
+        kq = cluster_min(k2);
+        if (CLUSTER) csync();
+      }
+      pivot_on(g, r, (int)kq.w2, c0, lc, cur);
+      ++pivots;
+    }
+  }
+
+  // Warm start: pivot each hinted structural column into the basis on the
+  // row, among rows whose basic variable is a slack the hint does not keep,
+  // with the largest |T_ij| (ties lowest row).  Returns how many hinted
+  // columns found no pivot (the hinted basis is singular on them).
+  __device__ int crash(const Geom& g, int c0, const int32_t* hint, const LpArgs& a,
+                       int& pivots, int cur, int lc) {
+    const T piv_tol = (T)a.piv_tol;
+    for (int i = threadIdx.x; i < g.m; i += blockDim.x) flags[i] = 0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < g.m; k += blockDim.x) {
+      const int h = hint[k];
+      if (h >= g.n && h < g.n + g.m) flags[h - g.n] = 1;
+    }
+    __syncthreads();
+    int missing = 0;
+    for (int k = 0; k < g.m; ++k) {
+      const int h = hint[k];
+      if (h < 0 || h >= g.n) continue;
+      bool isbasic = false;
+      for (int i = threadIdx.x; i < g.m; i += blockDim.x) isbasic = isbasic || basis[i] == h;
+      if (__syncthreads_or(isbasic ? 1 : 0)) continue;  // duplicate hint entry
+      const int owner = h / g.cw;
+      int r = -1;
+      if (owner == rank) {
+        Key kk = key_none();
+        const int hl = h - c0;
+        for (int i = threadIdx.x; i < g.m; i += blockDim.x) {
+          const int bi = basis[i];
+          if (bi >= g.n && bi < g.n + g.m && !flags[bi - g.n]) {
+            const T v = tab[(size_t)i * g.ldw + hl];
+            const T av = v < T(0) ? -v : v;
+            if (av > piv_tol) {
+              Key c = big_key(av, i, i);
+              if (key_less(c, kk)) kk = c;
+            }
+          }
+        }
+        kk = block_min(kk, redR);
+        r = kk.w2 == ~0u ? -1 : (int)kk.w3;
+        if (CLUSTER && threadIdx.x == 0) sh->r = r;
+      }
+      if (CLUSTER) {
+        csync();
+        if (owner != rank) r = remote(sh, owner)->r;
+        csync();
+      }
+      if (r < 0) {
+        ++missing;
+        continue;
+      }
+      pivot_on(g, r, h, c0, lc, cur);
+      ++pivots;
+    }
+    return missing;
+  }
+
+  // Tableau element (row i, global column j) wherever it lives.
+  __device__ T* elem(const Geom& g, int i, int j) {
+    const int o = j / g.cw;
+    T* p = tab + (size_t)i * g.ldw + (j - o * g.cw);
+    return o == rank ? p : remote(p, o);
+  }
+
+  // FP64 refresh of the FP32 tableau: x_B and the duals y are recomputed
+  // from the original A, b, c with one step of iterative refinement each
+  // (residual in FP64, correction through B^-1 = the slack columns of the
+  // tableau in FP32), then d_j = y^T a_j - c_j and z = c_B^T x_B in FP64.
+  // The FP32 RHS column (every replica) and objective row are overwritten.
+  // Rank 0 computes, reading and writing the other CTAs' columns through
+  // distributed shared memory.  Returns bit 0: x_B >= -ptol, bit 1:
+  // d >= -opt_tol (both judged in FP64).  Single-phase LPs only.
+  __device__ int refresh(const Geom& g, const double* A, const double* b, const double* c,
+                         const LpArgs& a) {
+    const int m = g.m, n = g.n;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    if (CLUSTER) csync();
+    int ok = 0;
+    if (rank == 0) {
+      double* res = reinterpret_cast<double*>(col0);  // col0|col1: m doubles
+      // Largest |correction| and |value| of a refinement step: positive
+      // floats order like their bit patterns, so a shared atomicMax works.
+      unsigned* mx = &sh->aux.w2;  // [0] max |correction|, [1] max |value|
+      for (int i = tid; i < m; i += nt) xr[i] = (double)tab[(size_t)i * g.ldw + g.cw];
+      for (int it = 0; it < 3; ++it) {
+        if (tid == 0) mx[0] = mx[1] = 0u;
+        __syncthreads();
+        for (int k = tid; k < m; k += nt) {
+          double r = b[k];
+          const double* Ak = A + (size_t)k * n;
+          for (int i = 0; i < m; ++i) {
+            const int bi = basis[i];
+            if (bi < n)
+              r = fma(-Ak[bi], xr[i], r);
+            else if (bi == n + k)
+              r = r - xr[i];
+          }
+          res[k] = r;
+        }
+        __syncthreads();
+        for (int i = warp; i < m; i += nw) {
+          float acc = 0.f;
+          for (int k = lane; k < m; k += 32)
+            acc = fmaf((float)*elem(g, i, n + k), (float)res[k], acc);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+          if (lane == 0) {
+            xr[i] += (double)acc;
+            atomicMax(&mx[0], __float_as_uint(fabsf(acc)));
+            atomicMax(&mx[1], __float_as_uint(fabsf((float)xr[i])));
+          }
+        }
+        __syncthreads();
+        if (__uint_as_float(mx[0]) <= 1e-12f * fmaxf(1.f, __uint_as_float(mx[1]))) break;
+        __syncthreads();
+      }
+      for (int k = tid; k < m; k += nt) yr[k] = (double)*elem(g, m, n + k);
+      for (int it = 0; it < 3; ++it) {
+        if (tid == 0) mx[0] = mx[1] = 0u;
+        __syncthreads();
+        for (int i = tid; i < m; i += nt) {
+          const int bi = basis[i];
+          double sres;
+          if (bi < n) {
+            sres = c[bi];
+            for (int k = 0; k < m; ++k) sres = fma(-A[(size_t)k * n + bi], yr[k], sres);
+          } else {
+            sres = -yr[bi - n];
+          }
+          res[i] = sres;
+        }
+        __syncthreads();
+        for (int k = tid; k < m; k += nt) {
+          float acc = 0.f;
+          for (int i = 0; i < m; ++i) acc = fmaf((float)res[i], (float)*elem(g, i, n + k), acc);
+          yr[k] += (double)acc;
+          atomicMax(&mx[0], __float_as_uint(fabsf(acc)));
+          atomicMax(&mx[1], __float_as_uint(fabsf((float)yr[k])));
+        }
+        __syncthreads();
+        if (__uint_as_float(mx[0]) <= 1e-12f * fmaxf(1.f, __uint_as_float(mx[1]))) break;
+        __syncthreads();
+      }
+      bool badd = false, badp = false;
+      for (int j = tid; j < n + m; j += nt) {
+        double d;
+        if (j < n) {
+          d = 0.0;
+          for (int k = 0; k < m; ++k) d = fma(A[(size_t)k * n + j], yr[k], d);
+          d = d - c[j];
+        } else {
+          d = yr[j - n];
+        }
+        *elem(g, m, j) = (T)d;
+        badd = badd || d < -a.opt_tol;
+      }
+      for (int i = tid; i < m; i += nt) {
+        const T xv = (T)xr[i];
+        for (int o = 0; o < K; ++o) {
+          T* p = tab + (size_t)i * g.ldw + g.cw;
+          *(o == rank ? p : remote(p, o)) = xv;
+        }
+        badp = badp || xr[i] < -a.ptol;
+      }
+      if (tid == 0) {
+        double z = 0.0;
+        for (int i = 0; i < m; ++i) {
+          const int bi = basis[i];
+          if (bi < n) z = fma(c[bi], xr[i], z);
+        }
+        sh->z = z;
+        for (int o = 0; o < K; ++o) {
+          T* p = tab + (size_t)m * g.ldw + g.cw;
+          *(o == rank ? p : remote(p, o)) = (T)z;
+        }
+      }
+      badd = __syncthreads_or(badd ? 1 : 0) != 0;
+      badp = __syncthreads_or(badp ? 1 : 0) != 0;
+      ok = (badp ? 0 : 1) | (badd ? 0 : 2);
+      if (tid == 0) sh->aux.w1 = (unsigned)ok;
+    }
+    if (CLUSTER) {
+      csync();
+      ok = (int)remote(&sh->aux, 0)->w1;
+      csync();
+    }
+    return ok;
+  }
+
+  // Build the slack-basis tableau of LP lp (rows with b_i < 0 negated, with
+  // an artificial column each); coalesced along rows of A.
+  __device__ void load(const Geom& g, int c0, int lc, const double* A, const double* b,
+                       const double* c) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int m = g.m, n = g.n, na = g.na;
+    const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+    for (int i = warp; i <= m; i += nw) {
+      const bool neg = i < m && b[i] < 0.0;
+      const T sgn = neg ? T(-1) : T(1);
+      int aidx = -1;
+      if (neg && na > 0) {
+        int cnt = 0;
+        for (int i2 = lane; i2 < i; i2 += 32) cnt += b[i2] < 0.0 ? 1 : 0;
+        cnt = __reduce_add_sync(0xffffffffu, cnt);
+        aidx = cnt;
+      }
+      T* row = tab + (size_t)i * g.ldw;
+      for (int lj = lane; lj < g.ldw; lj += 32) {
+        T v = T(0);
+        if (lj < lc) {
+          const int j = c0 + lj;
+          if (i < m) {
+            if (j < n) {
+              const T av = (T)A[(size_t)i * n + j];
+              v = neg ? -av : av;
+            } else if (j < n + m) {
+              v = (j - n == i) ? sgn : T(0);
+            } else {
+              v = (aidx >= 0 && j - n - m == aidx) ? T(1) : T(0);
+            }
+          } else if (na == 0 && j < n) {
+            v = -(T)c[j];
+          }
+        } else if (lj == g.cw && i < m) {
+          const T bv = (T)b[i];
+          v = neg ? -bv : bv;
+        }
+        row[lj] = v;
+      }
+      if (i < m && lane == 0) basis[i] = neg ? n + m + aidx : n + i;
+    }
+    __syncthreads();
+  }
+
   __device__ void run(const LpArgs& a, const ClassArgs& ca) {
     const int tid = threadIdx.x, nt = blockDim.x;
+    constexpr bool kFP32 = sizeof(T) == 4;
     for (;;) {
       if (rank == 0 && tid == 0) sh->ticket = atomicAdd(ca.ticket, 1);
       csync();
@@ -605,58 +972,18 @@ struct Solver {
           a.status[lp] = kUndef;
           a.obj[lp] = 0.0;
           if (a.pivots) a.pivots[lp] = -1;
+          if (a.info) a.info[lp] = 0;
         }
         __syncthreads();
         continue;
       }
       const int c0 = rank * g.cw;
       const int lc = max(0, min(g.cw, g.Wc - c0));
-      // load the slack-basis tableau (rows with b_i < 0 negated, with an
-      // artificial column each); coalesced along rows of A
-      const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
-      for (int i = warp; i <= m; i += nw) {
-        const bool neg = i < m && b[i] < 0.0;
-        const T sgn = neg ? T(-1) : T(1);
-        // index of this row's artificial column (rank among negative rows)
-        int aidx = -1;
-        if (neg && na > 0) {
-          int cnt = 0;
-          for (int i2 = lane; i2 < i; i2 += 32) cnt += b[i2] < 0.0 ? 1 : 0;
-          cnt = __reduce_add_sync(0xffffffffu, cnt);
-          aidx = cnt;
-        }
-        T* row = tab + (size_t)i * g.ldw;
-        for (int lj = lane; lj < g.ldw; lj += 32) {
-          T v = T(0);
-          if (lj < lc) {
-            const int j = c0 + lj;
-            if (i < m) {
-              if (j < n)
-                {
-                const T av = (T)A[(size_t)i * n + j];
-                v = neg ? -av : av;
-              }
-              else if (j < n + m)
-                v = (j - n == i) ? sgn : T(0);
-              else
-                v = (aidx >= 0 && j - n - m == aidx) ? T(1) : T(0);
-            } else if (na == 0 && j < n) {
-              v = -(T)c[j];
-            }
-          } else if (lj == g.cw && i < m) {
-            {
-            const T bv = (T)b[i];
-            v = neg ? -bv : bv;
-          }
-          }
-          row[lj] = v;
-        }
-        if (i < m && lane == 0) basis[i] = neg ? n + m + aidx : n + i;
-      }
-      __syncthreads();
-      int pivots = 0, degen = 0, cur = 0, st;
-      bool bland = false;
+      load(g, c0, lc, A, b, c);
+      int pivots = 0, degen = 0, cur = 0, st, info = 0;
+      bool bland = false, refreshed = false;
       const int max_piv = a.max_pivots > 0 ? a.max_pivots : 50 * (m + n) + 1000;
+      const T ptol = (T)a.ptol, opt_tol = (T)a.opt_tol;
       if (na > 0) {
         objective_row(g, c0, lc, c, true);
         __syncthreads();
@@ -677,14 +1004,94 @@ struct Solver {
           st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
         }
       } else {
-        st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
+        st = -1;
+        if (a.hint) {
+          info |= kInfoWarm;
+          if (crash(g, c0, a.hint + a.offbasis[lp], a, pivots, cur, lc) > 0) info |= kInfoPartial;
+          int fl;
+          if (kFP32) {
+            fl = refresh(g, A, b, c, a);
+            refreshed = true;
+            info |= kInfoRefresh;
+          } else {
+            fl = check_feasible(g, c0, lc, ptol, opt_tol);
+          }
+          if (fl & 1) {
+            st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
+          } else if (fl & 2) {
+            info |= kInfoDual;
+            st = dual_loop(g, c0, lc, a, max_piv, pivots, cur, ptol);
+            if (st == kOpt) st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
+          } else if (a.warm_mode == 1) {
+            // infeasible both ways: shift the costs of the columns with
+            // d_j < -opt_tol to small distinct positive values (dual
+            // feasible), dual simplex to a primal-feasible basis, restore the
+            // true costs, primal simplex
+            info |= kInfoDual | kInfoShift;
+            T* drow = tab + (size_t)m * g.ldw;
+            for (int lj = tid; lj < lc; lj += nt) {
+              const int j = c0 + lj;
+              if (j < n + m && drow[lj] < -opt_tol)
+                drow[lj] = (T)a.shift * (T(1) + (T)((j * 7919) % 1000) / T(1000));
+            }
+            __syncthreads();
+            st = dual_loop(g, c0, lc, a, max_piv, pivots, cur, ptol);
+            if (st == kOpt) {
+              objective_row(g, c0, lc, c, false);
+              __syncthreads();
+              st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
+            }
+          }
+          if (st < 0 || st == kNoFeas) {
+            // infeasible both ways (or dual simplex stuck): cold solve
+            info |= kInfoFallback;
+            if (CLUSTER) csync();
+            load(g, c0, lc, A, b, c);
+            refreshed = false;
+            bland = false;
+            degen = 0;
+            st = -1;
+          }
+        }
+        if (st < 0) {
+          const int period = kFP32 ? a.refresh_period : 0;
+          for (;;) {
+            st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur, period);
+            if (st != kRefresh) break;
+            if (CLUSTER) csync();
+            refresh(g, A, b, c, a);
+            refreshed = true;
+            info |= kInfoRefresh;
+          }
+        }
+        // FP32: verify the final basis in FP64 and repair if needed
+        if (kFP32 && st == kOpt) {
+          for (int round = 0; round < 4; ++round) {
+            if (CLUSTER) csync();
+            const int fl = refresh(g, A, b, c, a);
+            refreshed = true;
+            info |= kInfoRefresh;
+            if ((fl & 3) == 3) break;
+            info |= kInfoRepair;
+            if (!(fl & 1)) {
+              info |= kInfoDual;
+              st = dual_loop(g, c0, lc, a, max_piv, pivots, cur, ptol);
+              if (st != kOpt) break;
+            }
+            st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
+            if (st != kOpt) break;
+          }
+        }
       }
-      // outputs (rank 0 holds a replica of the RHS column)
+      if (CLUSTER) csync();
+      // outputs (rank 0 holds a replica of the RHS column; after an FP64
+      // refresh the FP64 x_B and objective are reported)
       if (rank == 0) {
         if (tid == 0) {
           a.status[lp] = st;
-          a.obj[lp] = (double)tab[(size_t)m * g.ldw + g.cw];
+          a.obj[lp] = refreshed ? sh->z : (double)tab[(size_t)m * g.ldw + g.cw];
           if (a.pivots) a.pivots[lp] = pivots;
+          if (a.info) a.info[lp] = info;
         }
         if (a.basis)
           for (int i = tid; i < m; i += nt) a.basis[a.offbasis[lp] + i] = basis[i];
@@ -693,7 +1100,8 @@ struct Solver {
           for (int j = tid; j < n; j += nt) x[j] = 0.0;
           __syncthreads();
           for (int i = tid; i < m; i += nt)
-            if (basis[i] < n) x[basis[i]] = (double)tab[(size_t)i * g.ldw + g.cw];
+            if (basis[i] < n)
+              x[basis[i]] = refreshed ? xr[i] : (double)tab[(size_t)i * g.ldw + g.cw];
         }
       }
       __syncthreads();
@@ -726,6 +1134,9 @@ __global__ void __launch_bounds__(512, 1) solve_kernel(const LpArgs a, const Cla
   s.col1 = reinterpret_cast<T*>(smem_raw + L.colB);
   s.rhsx = reinterpret_cast<T*>(smem_raw + L.rhsx);
   s.basis = reinterpret_cast<int*>(smem_raw + L.basis);
+  s.flags = reinterpret_cast<int*>(smem_raw + L.flags);
+  s.xr = reinterpret_cast<double*>(smem_raw + L.ext);
+  s.yr = s.xr + round_up(ca.max_m + 1, 4);
   s.redP = reinterpret_cast<Key*>(smem_raw + L.red);
   s.redR = s.redP + 32;
   s.redH = s.redP + 64;

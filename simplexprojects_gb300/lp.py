@@ -67,6 +67,13 @@ class LPBatch:
         A = self.A[oA[k]:oA[k] + m * n].reshape(m, n)
         return A, self.b[ob[k]:ob[k] + m], self.c[oc[k]:oc[k] + n]
 
+    def head(self, k: int) -> "LPBatch":
+        """The first k LPs, sharing this batch's arrays through offsets."""
+        oA, ob, oc = self.offsets()
+        fam = self.family[:k] if self.family is not None else None
+        return LPBatch(self.m[:k], self.n[:k], self.A, self.b, self.c, off_A=oA[:k],
+                       off_b=ob[:k], off_c=oc[:k], family=fam, meta=dict(self.meta, head=k))
+
     def subset(self, idx) -> "LPBatch":
         """A packed copy of the LPs listed in idx."""
         idx = np.asarray(idx, dtype=np.int64)
@@ -129,6 +136,11 @@ def generate(kind: int, count: Optional[int] = None, seed: int = DEFAULT_SEED, f
     L = N.lib()
     if count is None:
         count = WORKLOAD_COUNTS[kind]
+    if share_family_A and kind in (3, 4) and count > 2048:
+        # generate in chunks so that only one copy of each family's A exists
+        parts = [generate(kind, min(2048, count - k0), seed, first + k0, threads, True)
+                 for k0 in range(0, count, 2048)]
+        return _concat_shared(parts, dict(kind=kind, seed=seed, first=first, count=count))
     m = np.zeros(count, np.int32)
     n = np.zeros(count, np.int32)
     fam = np.zeros(count, np.int32)
@@ -147,6 +159,44 @@ def generate(kind: int, count: Optional[int] = None, seed: int = DEFAULT_SEED, f
     if share_family_A and (fam >= 0).any():
         batch = _share_family_A(batch)
     return batch
+
+
+def _concat_shared(parts, meta) -> LPBatch:
+    """Concatenate family-shared batches, keeping one A per family."""
+    As, fam_pos, pos = [], {}, 0
+    oAs, bs, cs, obs, ocs = [], [], [], [], []
+    bpos = cpos = 0
+    for p in parts:
+        oA, ob, oc = p.offsets()
+        newA = np.empty(p.count, np.int64)
+        local = {}
+        for k in range(p.count):
+            f = int(p.family[k])
+            src = int(oA[k])
+            if f >= 0 and f in fam_pos:
+                newA[k] = fam_pos[f]
+                continue
+            if src in local:
+                newA[k] = local[src]
+                continue
+            size = int(p.m[k]) * int(p.n[k])
+            As.append(p.A[src:src + size])
+            local[src] = pos
+            if f >= 0:
+                fam_pos[f] = pos
+            newA[k] = pos
+            pos += size
+        oAs.append(newA)
+        obs.append(ob + bpos)
+        ocs.append(oc + cpos)
+        bs.append(p.b)
+        cs.append(p.c)
+        bpos += p.b.size
+        cpos += p.c.size
+    return LPBatch(np.concatenate([p.m for p in parts]), np.concatenate([p.n for p in parts]),
+                   np.concatenate(As), np.concatenate(bs), np.concatenate(cs),
+                   off_A=np.concatenate(oAs), off_b=np.concatenate(obs), off_c=np.concatenate(ocs),
+                   family=np.concatenate([p.family for p in parts]), meta=dict(meta, shared_A=True))
 
 
 def _share_family_A(batch: LPBatch) -> LPBatch:

@@ -27,6 +27,7 @@ class SolveResult:
     pivots: Optional[np.ndarray] = None
     x: Optional[np.ndarray] = None
     basis: Optional[np.ndarray] = None
+    info: Optional[np.ndarray] = None
 
 
 def options(precision: str = "fp64", **kw) -> N.Options:
@@ -43,22 +44,29 @@ def options(precision: str = "fp64", **kw) -> N.Options:
 
 
 def solve(batch: LPBatch, precision: str = "fp64", want_x: bool = False,
-          want_basis: bool = False, **opts) -> SolveResult:
-    """Solve every LP of a host batch on the GPU (blocking)."""
+          want_basis: bool = False, hint: Optional[np.ndarray] = None, **opts) -> SolveResult:
+    """Solve every LP of a host batch on the GPU (blocking).  `hint` (optional)
+    is a packed array of m[k] basic column ids per LP (a warm-start basis)."""
     L = N.lib()
     k = batch.count
     st = np.zeros(k, np.int32)
     ob = np.zeros(k, np.float64)
     pv = np.zeros(k, np.int32)
+    info = np.zeros(k, np.int32)
     _, _, oc = batch.offsets()
     x = np.zeros(int(max((oc + batch.n).max(), 0)) if k else 0) if want_x else None
     bs = np.zeros(int(batch.m.sum()), np.int32) if want_basis else None
     res = N.Result(N.ptr(st, C.c_int32), N.ptr(ob, C.c_double), N.ptr(x, C.c_double),
-                   N.ptr(pv, C.c_int32), N.ptr(bs, C.c_int32))
+                   N.ptr(pv, C.c_int32), N.ptr(bs, C.c_int32), N.ptr(info, C.c_int32))
     o = options(precision, **opts)
+    if hint is not None:
+        hint = np.ascontiguousarray(hint, dtype=np.int32)
+        if hint.size != int(batch.m.sum()):
+            raise ValueError("hint must hold m[k] column ids per LP")
+        o.basis_hint = N.ptr(hint, C.c_int32)
     bst = batch.c_struct()
     N.check(L.blpg_solve_batch(C.byref(bst), C.byref(o), C.byref(res)), "blpg_solve_batch")
-    return SolveResult(st, ob, pv, x, bs)
+    return SolveResult(st, ob, pv, x, bs, info)
 
 
 class Plan:
@@ -95,11 +103,13 @@ class Plan:
         return int(self._L.blpg_plan_launches(self._h))
 
     def execute(self, dA: int, db: int, dc: int, status: int, objective: int, x: int = 0,
-                pivots: int = 0, basis: int = 0, stream: int = 0, basis_hint: int = 0) -> None:
+                pivots: int = 0, basis: int = 0, stream: int = 0, basis_hint: int = 0,
+                info: int = 0) -> None:
         """Enqueue a solve on raw device pointers (ints) on `stream`."""
         res = N.Result(C.cast(status, N.i32p), C.cast(objective, N.f64p),
                        C.cast(x, N.f64p) if x else None, C.cast(pivots, N.i32p) if pivots else None,
-                       C.cast(basis, N.i32p) if basis else None)
+                       C.cast(basis, N.i32p) if basis else None,
+                       C.cast(info, N.i32p) if info else None)
         N.check(self._L.blpg_plan_execute(self._h, dA, db, dc, basis_hint or None,
                                           C.byref(res), stream or None), "blpg_plan_execute")
 
@@ -138,8 +148,11 @@ class DeviceBatch:
                   if want_x else None)
         self.basis = (torch.zeros(int(batch.m.sum()), dtype=torch.int32, device=dev)
                       if want_basis else None)
+        self.info = torch.zeros(k, dtype=torch.int32, device=dev)
 
-    def run(self, stream=None) -> None:
+    def run(self, stream=None, hint=None) -> None:
+        """Enqueue one solve; `hint` is an optional int32 CUDA tensor of m[k]
+        basic column ids per LP (a warm-start basis)."""
         torch = self.torch
         s = stream if stream is not None else torch.cuda.current_stream()
         self.plan.execute(self.A.data_ptr(), self.b.data_ptr(), self.c.data_ptr(),
@@ -147,14 +160,17 @@ class DeviceBatch:
                           self.x.data_ptr() if self.x is not None else 0,
                           self.pivots.data_ptr(),
                           self.basis.data_ptr() if self.basis is not None else 0,
-                          stream=s.cuda_stream)
+                          stream=s.cuda_stream,
+                          basis_hint=hint.data_ptr() if hint is not None else 0,
+                          info=self.info.data_ptr())
 
     def result(self) -> SolveResult:
         self.torch.cuda.synchronize()
         return SolveResult(self.status.cpu().numpy(), self.objective.cpu().numpy(),
                            self.pivots.cpu().numpy(),
                            self.x.cpu().numpy() if self.x is not None else None,
-                           self.basis.cpu().numpy() if self.basis is not None else None)
+                           self.basis.cpu().numpy() if self.basis is not None else None,
+                           self.info.cpu().numpy())
 
 
 class Simplex:

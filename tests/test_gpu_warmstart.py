@@ -1,0 +1,133 @@
+"""GPU warm start from a basis hint, through the C ABI, against the oracle.
+
+The hinted structural columns are pivoted in (largest-magnitude pivot among
+rows whose slack the hint does not keep); the LP is then finished by primal
+simplex (hinted basis primal feasible), dual simplex (dual feasible), a
+cost-shifted dual phase (infeasible both ways, warm_mode 1, the default) or a
+cold solve (warm_mode 2).  FP64: bit-identical to the oracle's same path.
+"""
+import numpy as np
+import pytest
+
+import simplexprojects_gb300 as sp
+from oracle import ref
+
+pytestmark = pytest.mark.gpu
+
+
+def _hints(batch, cold_basis):
+    m = batch.m
+    B = np.split(cold_basis, np.cumsum(m)[:-1])
+    k = batch.count
+    rng = np.random.default_rng(7)
+    perfect = cold_basis.copy()
+    sibling = np.concatenate([B[(i + 64) % k] for i in range(k)])  # same family
+    rand = np.concatenate([rng.permutation(int(m[i]) + int(batch.n[i]))[: int(m[i])]
+                           for i in range(k)]).astype(np.int32)
+    return {"perfect": perfect, "sibling": sibling, "random": rand}
+
+
+@pytest.fixture(scope="module")
+def fam_batch():
+    return sp.generate(3, 192, seed=sp.DEFAULT_SEED + 1, share_family_A=True)
+
+
+@pytest.mark.parametrize("mode,oracle_composite", [(1, 1), (2, 0)])
+def test_warm_fp64_bit_identical(built, fam_batch, mode, oracle_composite):
+    cold = ref.solve_batch(fam_batch, "fp64", want_basis=True)
+    for name, hint in _hints(fam_batch, cold.basis).items():
+        g = sp.solve(fam_batch, "fp64", want_x=True, want_basis=True, hint=hint, warm_mode=mode)
+        c = ref.solve_batch(fam_batch, "fp64", want_x=True, want_basis=True, hint=hint,
+                            composite=oracle_composite)
+        assert np.array_equal(g.status, c.status), name
+        assert np.array_equal(g.pivots, c.pivots), name
+        assert np.array_equal(g.info, c.info), name
+        assert np.array_equal(g.basis, c.basis), name
+        assert np.array_equal(g.objective.view(np.uint64), c.objective.view(np.uint64)), name
+        assert np.array_equal(g.status, cold.status), name
+    # a perfect hint needs only the crash pivots (one per structural basic)
+    g = sp.solve(fam_batch, "fp64", hint=cold.basis)
+    nstruct = np.array([(b < n).sum() for b, n in
+                        zip(np.split(cold.basis, np.cumsum(fam_batch.m)[:-1]), fam_batch.n)])
+    assert np.array_equal(g.pivots, nstruct)
+
+
+def test_warm_fp32_matches_exact(built, fam_batch):
+    cold = ref.solve_batch(fam_batch, "fp64", want_basis=True)
+    for name, hint in _hints(fam_batch, cold.basis).items():
+        g = sp.solve(fam_batch, "fp32", hint=hint)
+        assert np.array_equal(g.status, cold.status), name
+        opt = cold.status == 5
+        rel = np.abs(g.objective[opt] - cold.objective[opt]) / np.abs(cold.objective[opt])
+        assert rel.max() <= 1e-6, (name, rel.max())  # the FP32 form's bar
+        assert (g.info[opt] & 16).all()  # refreshed in FP64 at termination
+
+
+def test_warm_cluster_split_fp64(built):
+    """Warm start on LPs split across a cluster (the crash and dual phases
+    exchange pivot rows and columns through distributed shared memory)."""
+    batch = sp.generate(3, 24, seed=11, share_family_A=True)
+    cold = ref.solve_batch(batch, "fp64", want_basis=True)
+    hint = _hints(batch, cold.basis)["random"]
+    for K in (2, 4):
+        g = sp.solve(batch, "fp64", want_basis=True, hint=hint, min_cluster=K)
+        c = ref.solve_batch(batch, "fp64", want_basis=True, hint=hint)
+        assert np.array_equal(g.pivots, c.pivots) and np.array_equal(g.basis, c.basis)
+        assert np.array_equal(g.objective.view(np.uint64), c.objective.view(np.uint64))
+
+
+def test_hint_ignored_for_two_phase_lps(built, known_golden):
+    lps = [(v["A"], v["b"], v["c"]) for v in known_golden["hand"].values()]
+    batch = sp.LPBatch.from_lps(lps)
+    hint = np.concatenate([np.arange(len(v["b"])) for v in known_golden["hand"].values()])
+    g = sp.solve(batch, "fp64", hint=hint.astype(np.int32))
+    c = ref.solve_batch(batch, "fp64", hint=hint.astype(np.int32))
+    assert np.array_equal(g.status, c.status) and np.array_equal(g.pivots, c.pivots)
+    assert np.array_equal(g.objective.view(np.uint64), c.objective.view(np.uint64))
+
+
+def test_learned_warm_start_end_to_end(built):
+    """Train the network on plain-solver bases of 4,096 perturbed LPs, then
+    solve 512 held-out LPs with its hints: fewer pivots than the cold solve
+    (what the network gains over the method without it), identical statuses,
+    FP64 results bit-identical to the oracle given the same hints, FP32
+    objectives within 1e-6."""
+    from simplexprojects_gb300.warmstart import WarmStart, LearnedSolver, basis_accuracy
+    train = sp.generate(3, 4096, seed=sp.DEFAULT_SEED, first=0, share_family_A=True)
+    held = sp.generate(3, 512, seed=sp.DEFAULT_SEED, first=45_000, share_family_A=True)
+    tb = sp.solve(train, "fp64", want_basis=True)
+    ws = WarmStart(174, 142, 64, seed=3)
+    rep = ws.train(train, tb.basis, epochs=8, lr=1e-3)
+    assert rep.losses[-1] < rep.losses[0]
+    cold = sp.solve(held, "fp64", want_basis=True)
+    ls = LearnedSolver(ws, held, "fp64")
+    ls.run()
+    res = ls.result()
+    hint = ls.hint.cpu().numpy()
+    acc, _ = basis_accuracy(hint, cold.basis, 174)
+    assert acc > 0.8
+    assert np.array_equal(res.status, cold.status)
+    assert res.pivots.mean() < cold.pivots.mean()
+    orc = ref.solve_batch(held, "fp64", hint=hint)
+    assert np.array_equal(res.pivots, orc.pivots) and np.array_equal(res.info, orc.info)
+    assert np.array_equal(res.objective.view(np.uint64), orc.objective.view(np.uint64))
+    l32 = LearnedSolver(ws, held, "fp32")
+    r32 = l32.solve(held)
+    assert np.array_equal(r32.status, cold.status)
+    opt = cold.status == 5
+    rel = np.abs(r32.objective[opt] - cold.objective[opt]) / np.abs(cold.objective[opt])
+    assert rel.max() <= 1e-6
+
+
+def test_warm_start_checkpoint_roundtrip(built, tmp_path):
+    from simplexprojects_gb300.warmstart import WarmStart
+    train = sp.generate(3, 256, seed=5, share_family_A=True)
+    tb = sp.solve(train, "fp64", want_basis=True)
+    ws = WarmStart(174, 142, 64, hidden=128, layers=2, seed=1)
+    ws.train(train, tb.basis, epochs=1)
+    ws.save(str(tmp_path / "model"))
+    ws2 = WarmStart.load(str(tmp_path / "model"))
+    assert np.array_equal(ws.mlp.get_params(), ws2.mlp.get_params())
+    d = ws.device_inputs(train)
+    import torch
+    assert torch.equal(ws.features(d), ws2.features(d))
