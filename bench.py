@@ -210,7 +210,9 @@ def run_learned(args, rank, world, local):
     torch.cuda.synchronize()
     with Clocks(local) as clk:
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("timed_region")
         t_learned = timed(ls.run, args.steps)
+        torch.cuda.nvtx.range_pop()
     t_plain = timed(plain.run, args.steps)
     ls.predict()
     t_solve = timed(lambda: ls.db.run(hint=ls.hint), args.steps)  # the FP32 solve kernels alone

@@ -115,8 +115,9 @@ typedef struct blpg_options {
   int32_t min_cluster;     /* smallest cluster used even when one CTA would
                               do (tests of the cluster path); 0 = 1 */
   int32_t cta_smem_budget; /* shared memory per CTA that picks each LP's
-                              cluster size; 0 = autotuned (default: half an
-                              SM, i.e. two CTAs per SM) */
+                              cluster size; 0 = the tuning table's value,
+                              else the whole per-CTA shared memory (the
+                              fewest CTAs per LP) */
   int32_t ratio_rule;      /* 0 (default): Harris two-pass ratio test (largest
                               pivot among rows within the feas_tol-relaxed
                               step); 1: textbook minimum ratio.  Bland mode

@@ -177,7 +177,7 @@ static int pick_threads(const Geom& g, int precision, int K, int override_nt) {
     int nt = dev::round_up(std::max(override_nt, g.nl), 32);
     return std::min(nt, kMaxThreads);
   }
-  int floor_threads = precision == BLPG_FP64 ? 256 : 512;
+  int floor_threads = 512;
   {
     std::lock_guard<std::mutex> lk(g_tuning.mu);
     auto it = g_tuning.threads.find({precision * 16 + K, 0});
@@ -202,7 +202,10 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
   if (budget <= 0) {
     std::lock_guard<std::mutex> lk(g_tuning.mu);
     auto it = g_tuning.threads.find({p->precision * 16 + 15, 1});
-    budget = it != g_tuning.threads.end() ? it->second : (228 * 1024) / 2 - 1024;
+    // default: the whole per-CTA shared memory, i.e. the fewest CTAs per LP
+    // (measured on GB300: cluster barriers and DSMEM exchanges cost more
+    // than the occupancy they buy)
+    budget = it != g_tuning.threads.end() ? it->second : max_smem;
   }
   budget = std::min(budget, max_smem);
   const int min_cluster = std::max(1, std::min(p->opt.min_cluster, max_cluster));
@@ -388,7 +391,8 @@ extern "C" int32_t blpg_set_tuning(const char* json) {
   std::lock_guard<std::mutex> lk(g_tuning.mu);
   g_tuning.threads.clear();
   if (!json) return BLPG_OK;
-  // Minimal reader for {"fp64_k1": 256, "fp32_k2": 512, ...}
+  // Minimal reader for {"fp64_k1": 256, "fp32_k2": 512, "fp64_smem": 115712, ...}:
+  // threads per CTA per (precision, cluster size) and the CTA smem budget.
   const char* s = json;
   while ((s = std::strchr(s, '"'))) {
     const char* e = std::strchr(s + 1, '"');
@@ -401,10 +405,8 @@ extern "C" int32_t blpg_set_tuning(const char* json) {
     if (std::sscanf(key.c_str(), "fp64_k%d", &K) == 1) prec = BLPG_FP64;
     else if (std::sscanf(key.c_str(), "fp32_k%d", &K) == 1) prec = BLPG_FP32;
     if (prec >= 0 && val > 0 && val <= 1024) g_tuning.threads[{prec * 16 + K, 0}] = val;
-    if (std::sscanf(key.c_str(), "fp64_smem%d", &K) == 1 && val > 0)
-      g_tuning.threads[{BLPG_FP64 * 16 + 15, 1}] = val;
-    if (std::sscanf(key.c_str(), "fp32_smem%d", &K) == 1 && val > 0)
-      g_tuning.threads[{BLPG_FP32 * 16 + 15, 1}] = val;
+    if (key == "fp64_smem" && val > 0) g_tuning.threads[{BLPG_FP64 * 16 + 15, 1}] = val;
+    if (key == "fp32_smem" && val > 0) g_tuning.threads[{BLPG_FP32 * 16 + 15, 1}] = val;
     s = colon + 1;
   }
   return BLPG_OK;

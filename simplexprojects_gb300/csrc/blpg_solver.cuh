@@ -145,7 +145,7 @@ struct Layout {
     red = off;
     off += 3 * 32 * 16;  // three argmin scratch buffers (pricing, ratio, Harris)
     state = off;
-    off += 80;
+    off += 224;
     total = off;
   }
 };
@@ -275,7 +275,9 @@ struct SharedState {
   double theta;
   Key pslot;
   Key aux;
-  double z;  // FP64 objective of the last refresh
+  double z;       // FP64 objective of the last refresh
+  double pad2;
+  Key gather[8];  // the cluster's pricing candidates, fetched once per CTA
 };
 
 // ---------------------------------------------------------------------------
@@ -320,9 +322,12 @@ struct Solver {
     if (!CLUSTER) return mine;
     if (threadIdx.x == 0) sh->pslot = mine;
     csync();
+    // K threads fetch one remote candidate each; the CTA reduces locally
+    if (threadIdx.x < K) sh->gather[threadIdx.x] = *remote(&sh->pslot, threadIdx.x);
+    __syncthreads();
     Key best = key_none();
     for (int k = 0; k < K; ++k) {
-      Key o = *remote(&sh->pslot, k);
+      const Key o = sh->gather[k];
       if (key_less(o, best)) best = o;
     }
     return best;
@@ -444,36 +449,58 @@ struct Solver {
 
   // Rank-1 update of rows 0..m-1 except r; the owner of the next column qn
   // extracts it into colx_next, every CTA extracts its RHS replica.
-  __device__ void update_body(const Geom& g, int r, const T* pcol, int qn,
-                              int owner_n, int c0, T* colx_next) {
+  __device__ void update_body(const Geom& g, int r, const T* pcol, int qn, int owner_n, int c0,
+                              T* colx_next) {
+    update_rows(tab, rhsx, rank, g.m, g.ldw, g.nl, g.cw, r, pcol, qn, owner_n, c0, colx_next);
+  }
+  // Kept out of line with plain arguments (no `this`, no structs by
+  // reference) so that the unrolled sweep has its own register budget and
+  // nothing in its loop lives in local memory.
+  static __device__ __noinline__ void update_rows(T* const tb, T* const rhsx, const int rank,
+                                                  const int m, const int ldw, const int nl,
+                                                  const int cw, const int r, const T* pcol,
+                                                  const int qn, const int owner_n, const int c0,
+                                                  T* colx_next) {
     const int nt = (int)blockDim.x;
-    const int G = nt / g.nl;
-    const int grp = threadIdx.x / g.nl;
-    const int lane = threadIdx.x - grp * g.nl;
+    const int G = nt / nl;
+    const int grp = threadIdx.x / nl;
+    const int lane = threadIdx.x - grp * nl;
     if (grp >= G) return;
-    const VT p = *reinterpret_cast<const VT*>(tab + (size_t)r * g.ldw + lane * V);
+    const VT p = *reinterpret_cast<const VT*>(tb + (size_t)r * ldw + lane * V);
     const int qloc = qn - c0;
     const bool has_q = qn >= 0 && owner_n == rank && (qloc / V) == lane;
     const int qe = qloc - lane * V;
-    const bool has_rhs = lane == g.cw / V;
-    for (int i = grp; i < g.m; i += G) {
-      VT t;
-      if (i != r) {
-        const T f = pcol[i];
-        VT* tp = reinterpret_cast<VT*>(tab + (size_t)i * g.ldw + lane * V);
-        if (f != T(0)) {
-          t = v_fma(f, p, *tp);
-          *tp = t;
-        } else {
-          t = *tp;  // fma(-0, p, t) would only flip the sign of a zero t
+    const bool has_rhs = lane == cw / V;
+    // kU rows per step, every load issued before any store (rows
+    // grp, grp + G, ... are disjoint, so this only adds memory parallelism)
+    constexpr int kU = 1;  // measured: deeper unrolling of the sweep is slower
+    for (int i0 = grp; i0 < m; i0 += kU * G) {
+      T f[kU];
+      VT t[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int i = i0 + u * G;
+        if (i < m) {
+          f[u] = pcol[i];
+          t[u] = *reinterpret_cast<const VT*>(tb + (size_t)i * ldw + lane * V);
         }
-      } else {
-        t = p;
       }
-      if (has_q) colx_next[i] = vget<VT, T>(t, qe);
-      if (has_rhs) rhsx[i] = vget<VT, T>(t, 0);
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int i = i0 + u * G;
+        if (i < m) {
+          if (i == r) {
+            t[u] = p;
+          } else if (f[u] != T(0)) {  // a zero multiplier leaves the row as it is
+            t[u] = v_fma(f[u], p, t[u]);
+            *reinterpret_cast<VT*>(tb + (size_t)i * ldw + lane * V) = t[u];
+          }
+          if (has_q) colx_next[i] = vget<VT, T>(t[u], qe);
+          if (has_rhs) rhsx[i] = vget<VT, T>(t[u], 0);
+        }
+      }
     }
-    if (has_q && grp == 0) colx_next[g.m] = tab[(size_t)g.m * g.ldw + qloc];
+    if (has_q && grp == 0) colx_next[m] = tb[(size_t)m * ldw + qloc];
   }
 
   // The primal simplex loop from the current tableau (the oracle's
@@ -505,17 +532,21 @@ struct Solver {
       if (CLUSTER) {
         csync();  // B1
         if (owner != rank) {
-          const SharedState* os = remote(sh, owner);
-          r = os->r;
-          theta = (T)os->theta;
+          // one thread fetches the owner's verdict; every thread copies part
+          // of the pivot column (unused if the LP turns out unbounded)
+          if (threadIdx.x == 0) {
+            const SharedState* os = remote(sh, owner);
+            sh->r = os->r;
+            sh->theta = os->theta;
+          }
+          const T* src = remote(colbuf(cur), owner);
+          for (int i = threadIdx.x; i <= g.m; i += blockDim.x) colbuf(cur)[i] = src[i];
+          __syncthreads();
+          r = sh->r;
+          theta = (T)sh->theta;
         }
       }
       if (r < 0) return kUnbnd;
-      if (CLUSTER && owner != rank) {
-        const T* src = remote(colbuf(cur), owner);
-        for (int i = threadIdx.x; i <= g.m; i += blockDim.x) colbuf(cur)[i] = src[i];
-        __syncthreads();
-      }
       if (theta <= deg_tol) {
         if (++degen > a.bland_after) bland = true;
       } else {
@@ -771,6 +802,7 @@ struct Solver {
 
   // Tableau element (row i, global column j) wherever it lives.
   __device__ T* elem(const Geom& g, int i, int j) {
+    if (!CLUSTER) return tab + (size_t)i * g.ldw + j;
     const int o = j / g.cw;
     T* p = tab + (size_t)i * g.ldw + (j - o * g.cw);
     return o == rank ? p : remote(p, o);
@@ -793,24 +825,74 @@ struct Solver {
     int ok = 0;
     if (rank == 0) {
       double* res = reinterpret_cast<double*>(col0);  // col0|col1: m doubles
+      // Structural basics as a compact list (row, column); for every slack
+      // the row where it is basic (-1 when nonbasic).  flags[] holds the
+      // list (its warm-start use is over by now), slackrow aliases yr until
+      // the duals are needed.
+      int* slist = flags;
+      int* slackrow = reinterpret_cast<int*>(yr);
+      int* wcount = reinterpret_cast<int*>(redH);  // per-32-row chunk counts (<= 128)
+      const int nchunks = ceil_div(m, 32);
+      for (int k = tid; k < m; k += nt) slackrow[k] = -1;
+      // row-ordered compaction: ballot per 32-row chunk, then a prefix sum
+      for (int ch = warp; ch < nchunks; ch += nw) {
+        const int i = ch * 32 + lane;
+        const bool st = i < m && basis[i] < n;
+        const unsigned bal = __ballot_sync(0xffffffffu, st);
+        if (lane == 0) wcount[ch] = __popc(bal);
+        if (i < m && !st && basis[i] < n + m) slackrow[basis[i] - n] = i;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        int acc = 0;
+        for (int ch = 0; ch < nchunks; ++ch) {
+          const int v = wcount[ch];
+          wcount[ch] = acc;
+          acc += v;
+        }
+        wcount[nchunks] = acc;
+      }
+      __syncthreads();
+      for (int ch = warp; ch < nchunks; ch += nw) {
+        const int i = ch * 32 + lane;
+        const bool st = i < m && basis[i] < n;
+        const unsigned bal = __ballot_sync(0xffffffffu, st);
+        if (st) slist[wcount[ch] + __popc(bal & ((1u << lane) - 1u))] = i;
+      }
+      __syncthreads();
+      const int ns = wcount[nchunks];
       // Largest |correction| and |value| of a refinement step: positive
       // floats order like their bit patterns, so a shared atomicMax works.
       unsigned* mx = &sh->aux.w2;  // [0] max |correction|, [1] max |value|
       for (int i = tid; i < m; i += nt) xr[i] = (double)tab[(size_t)i * g.ldw + g.cw];
-      for (int it = 0; it < 3; ++it) {
+      for (int it = 0; it < 2; ++it) {
         if (tid == 0) mx[0] = mx[1] = 0u;
         __syncthreads();
-        for (int k = tid; k < m; k += nt) {
-          double r = b[k];
-          const double* Ak = A + (size_t)k * n;
-          for (int i = 0; i < m; ++i) {
-            const int bi = basis[i];
-            if (bi < n)
-              r = fma(-Ak[bi], xr[i], r);
-            else if (bi == n + k)
-              r = r - xr[i];
+        // res_k = b_k - sum over structural basics A_k,bi x_i - x_(slack k)
+        // four threads per row k (a quad of lanes), each summing every 4th
+        // structural basic; the quad combines in a fixed order
+        // warp-uniform trip count: every lane reaches the shuffles
+        for (int wb = tid & ~31; wb < 4 * m; wb += nt) {
+          const int k = (wb + lane) >> 2, q = lane & 3;
+          double part = 0.0;
+          if (k < m) {
+            const double* Ak = A + (size_t)k * n;
+#pragma unroll 4
+            for (int t = q; t < ns; t += 4) {
+              const int i = slist[t];
+              part = fma(Ak[basis[i]], xr[i], part);
+            }
           }
-          res[k] = r;
+          const double p1 = __shfl_xor_sync(0xffffffffu, part, 1);
+          const double s01 = (q & 1) ? p1 + part : part + p1;
+          const double p2 = __shfl_xor_sync(0xffffffffu, s01, 2);
+          const double sum = (q & 2) ? p2 + s01 : s01 + p2;
+          if (k < m && q == 0) {
+            double r = b[k] - sum;
+            const int sr = slackrow[k];
+            if (sr >= 0) r = r - xr[sr];
+            res[k] = r;
+          }
         }
         __syncthreads();
         for (int i = warp; i < m; i += nw) {
@@ -826,47 +908,87 @@ struct Solver {
           }
         }
         __syncthreads();
-        if (__uint_as_float(mx[0]) <= 1e-12f * fmaxf(1.f, __uint_as_float(mx[1]))) break;
+        if (__uint_as_float(mx[0]) <= 1e-10f * fmaxf(1.f, __uint_as_float(mx[1]))) break;
         __syncthreads();
       }
+      __syncthreads();  // slackrow (aliasing yr) no longer needed
       for (int k = tid; k < m; k += nt) yr[k] = (double)*elem(g, m, n + k);
-      for (int it = 0; it < 3; ++it) {
+      for (int it = 0; it < 2; ++it) {
         if (tid == 0) mx[0] = mx[1] = 0u;
         __syncthreads();
+        // s_i = cB_i - (B^T y)_i: slack basics -y_(bi-n); structural basics
+        // c_bi - A_(:,bi)^T y, one warp per column (lanes over rows)
         for (int i = tid; i < m; i += nt) {
           const int bi = basis[i];
-          double sres;
-          if (bi < n) {
-            sres = c[bi];
-            for (int k = 0; k < m; ++k) sres = fma(-A[(size_t)k * n + bi], yr[k], sres);
-          } else {
-            sres = -yr[bi - n];
-          }
-          res[i] = sres;
+          if (bi >= n) res[i] = bi < n + m ? -yr[bi - n] : 0.0;
+        }
+        for (int t = warp; t < ns; t += nw) {
+          const int i = slist[t], bi = basis[i];
+          double acc = 0.0;
+#pragma unroll 4
+          for (int k = lane; k < m; k += 32) acc = fma(A[(size_t)k * n + bi], yr[k], acc);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+          if (lane == 0) res[i] = c[bi] - acc;
         }
         __syncthreads();
-        for (int k = tid; k < m; k += nt) {
+        // dy_k = sum_i s_i Binv_ik.  With m <= 192 two halves of the rows per
+        // column are summed by separate threads into the (idle) argmin
+        // scratch and combined in a fixed order; larger m in one pass.
+        float* half = reinterpret_cast<float*>(redP);  // 1536 B: 2 x m floats for m <= 192
+        const int H = 2 * m <= 3 * 32 * 4 ? 2 : 1;
+        const int mh = (m + H - 1) / H;
+        for (int w = tid; w < H * m; w += nt) {
+          const int k = w % m, h = w / m;
+          const int i0 = h * mh, i1 = min(m, i0 + mh);
           float acc = 0.f;
-          for (int i = 0; i < m; ++i) acc = fmaf((float)res[i], (float)*elem(g, i, n + k), acc);
-          yr[k] += (double)acc;
-          atomicMax(&mx[0], __float_as_uint(fabsf(acc)));
-          atomicMax(&mx[1], __float_as_uint(fabsf((float)yr[k])));
+#pragma unroll 4
+          for (int i = i0; i < i1; ++i) acc = fmaf((float)res[i], (float)*elem(g, i, n + k), acc);
+          if (H == 2) {
+            half[h * m + k] = acc;
+          } else {
+            yr[k] += (double)acc;
+            atomicMax(&mx[0], __float_as_uint(fabsf(acc)));
+            atomicMax(&mx[1], __float_as_uint(fabsf((float)yr[k])));
+          }
         }
         __syncthreads();
-        if (__uint_as_float(mx[0]) <= 1e-12f * fmaxf(1.f, __uint_as_float(mx[1]))) break;
+        if (H == 2) {
+          for (int k = tid; k < m; k += nt) {
+            const float acc = half[k] + half[m + k];
+            yr[k] += (double)acc;
+            atomicMax(&mx[0], __float_as_uint(fabsf(acc)));
+            atomicMax(&mx[1], __float_as_uint(fabsf((float)yr[k])));
+          }
+          __syncthreads();
+        }
+        if (__uint_as_float(mx[0]) <= 1e-10f * fmaxf(1.f, __uint_as_float(mx[1]))) break;
         __syncthreads();
       }
+      // Reduced costs d_j = y^T a_j - c_j for structural j: a quad of lanes
+      // per column, lane q summing rows q, q + 4, ...; the quad combines in a
+      // fixed order and its first lane writes d_j.  Slack k: d = y_k.
       bool badd = false, badp = false;
-      for (int j = tid; j < n + m; j += nt) {
-        double d;
+      for (int wb = tid & ~31; wb < 4 * n; wb += nt) {  // warp-uniform trip count
+        const int j = (wb + lane) >> 2, q = lane & 3;
+        double part = 0.0;
         if (j < n) {
-          d = 0.0;
-          for (int k = 0; k < m; ++k) d = fma(A[(size_t)k * n + j], yr[k], d);
-          d = d - c[j];
-        } else {
-          d = yr[j - n];
+#pragma unroll 8
+          for (int k = q; k < m; k += 4) part = fma(A[(size_t)k * n + j], yr[k], part);
         }
-        *elem(g, m, j) = (T)d;
+        const double p1 = __shfl_xor_sync(0xffffffffu, part, 1);
+        const double s01 = (q & 1) ? p1 + part : part + p1;
+        const double p2 = __shfl_xor_sync(0xffffffffu, s01, 2);
+        const double sum = (q & 2) ? p2 + s01 : s01 + p2;
+        if (j < n && q == 0) {
+          const double d = sum - c[j];
+          *elem(g, m, j) = (T)d;
+          badd = badd || d < -a.opt_tol;
+        }
+      }
+      for (int k = tid; k < m; k += nt) {
+        const double d = yr[k];
+        *elem(g, m, n + k) = (T)d;
         badd = badd || d < -a.opt_tol;
       }
       for (int i = tid; i < m; i += nt) {
@@ -953,7 +1075,12 @@ struct Solver {
     for (;;) {
       if (rank == 0 && tid == 0) sh->ticket = atomicAdd(ca.ticket, 1);
       csync();
-      const int t = *remote(&sh->ticket, 0);
+      if (CLUSTER) {
+        // rank 0 drew the ticket: one thread per CTA fetches it
+        if (rank != 0 && tid == 0) sh->ticket = remote(sh, 0)->ticket;
+        __syncthreads();
+      }
+      const int t = sh->ticket;
       if (t >= ca.count) break;
       const int lp = ca.order[t];
       const int m = a.m[lp], n = a.n[lp];

@@ -174,12 +174,13 @@ class WarmStart:
         """Fit the network on LPs with known optimal bases (packed m per LP)."""
         torch = self.torch
         bs = batch_size or self.mlp.max_batch
+        bs = max(64, min(bs, batch.count // 64 * 64))
         t0 = time.perf_counter()
         self.fit_stats(batch)
         X = self.features(self.device_inputs(batch))
         Y = self.labels(basis, batch.count)
         k = batch.count
-        steps = k // bs
+        steps = max(1, k // bs)
         rng = np.random.default_rng(seed)
         rep = TrainReport(epochs, 0.0, train_lps=k)
         for ep in range(epochs):
@@ -189,7 +190,7 @@ class WarmStart:
                 idx = perm[s * bs:(s + 1) * bs]
                 tot += self.mlp.train_step(X.index_select(0, idx).contiguous(),
                                            Y.index_select(0, idx).contiguous(), lr)
-            rep.losses.append(tot / (steps * bs * self.nf))
+            rep.losses.append(tot / max(1, steps * bs * self.nf))
             if log:
                 log(f"epoch {ep}: mean BCE {rep.losses[-1]:.4f}")
         torch.cuda.synchronize()

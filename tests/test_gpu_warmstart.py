@@ -93,11 +93,11 @@ def test_learned_warm_start_end_to_end(built):
     FP64 results bit-identical to the oracle given the same hints, FP32
     objectives within 1e-6."""
     from simplexprojects_gb300.warmstart import WarmStart, LearnedSolver, basis_accuracy
-    train = sp.generate(3, 4096, seed=sp.DEFAULT_SEED, first=0, share_family_A=True)
+    train = sp.generate(3, 16384, seed=sp.DEFAULT_SEED, first=0, share_family_A=True)
     held = sp.generate(3, 512, seed=sp.DEFAULT_SEED, first=45_000, share_family_A=True)
     tb = sp.solve(train, "fp64", want_basis=True)
     ws = WarmStart(174, 142, 64, seed=3)
-    rep = ws.train(train, tb.basis, epochs=8, lr=1e-3)
+    rep = ws.train(train, tb.basis, epochs=16, lr=1e-3)
     assert rep.losses[-1] < rep.losses[0]
     cold = sp.solve(held, "fp64", want_basis=True)
     ls = LearnedSolver(ws, held, "fp64")
@@ -105,9 +105,10 @@ def test_learned_warm_start_end_to_end(built):
     res = ls.result()
     hint = ls.hint.cpu().numpy()
     acc, _ = basis_accuracy(hint, cold.basis, 174)
-    assert acc > 0.8
+    assert acc > 0.85  # (an all-slack guess scores about 0.8)
+    assert (hint < 142).sum() > 20 * held.count  # structural columns are predicted
     assert np.array_equal(res.status, cold.status)
-    assert res.pivots.mean() < cold.pivots.mean()
+    assert res.pivots.mean() < 0.9 * cold.pivots.mean()
     orc = ref.solve_batch(held, "fp64", hint=hint)
     assert np.array_equal(res.pivots, orc.pivots) and np.array_equal(res.info, orc.info)
     assert np.array_equal(res.objective.view(np.uint64), orc.objective.view(np.uint64))
