@@ -184,8 +184,9 @@ def run_learned(args, rank, world, local):
     train = sp.generate(3, 40_000, seed=sp.DEFAULT_SEED, first=0, share_family_A=True)
     evalb = sp.generate(3, n_eval, seed=sp.DEFAULT_SEED, first=lo, share_family_A=True)
     tb = sp.solve(train, "fp64", want_basis=True)  # plain FP64 solver labels its own bases
-    ws = WarmStart(174, 142, 64, seed=7, device=dev)
-    rep = ws.train(train, tb.basis, epochs=args.epochs, lr=1e-3)
+    # inference runs the whole evaluation batch as one chunk (one GEMM per layer)
+    ws = WarmStart(174, 142, 64, seed=7, device=dev, max_batch=(max(n_eval, 1) + 63) // 64 * 64)
+    rep = ws.train(train, tb.basis, epochs=args.epochs, lr=1e-3, batch_size=512)
     del train
     ls = LearnedSolver(ws, evalb, "fp32")
     plain = sp.DeviceBatch(evalb, "fp64", device=dev)
@@ -288,7 +289,7 @@ def run_learned(args, rank, world, local):
                                   "frac": ach_tf / f32.value, "pipe": "fp32"}},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
-        "gpu_launches": args.steps * (ls.db.plan.launches() + 4 + 4 * ws.mlp.layers + 4),
+        "gpu_launches": args.steps * (ls.db.plan.launches() + ws.hint_launches(n_eval)),
         "step_ms_all": t_learned,
     }
     print(json.dumps(out))

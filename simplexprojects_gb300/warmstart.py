@@ -70,6 +70,12 @@ class MLP:
                                            C.byref(loss), s), "blpg_mlp_train_step")
         return loss.value
 
+    def predict_launches(self, rows: int) -> int:
+        """Kernels one predict() of `rows` rows launches: per chunk of at most
+        max_batch rows, one BF16 conversion and layers + 1 GEMMs."""
+        chunks = (rows + self.max_batch - 1) // self.max_batch
+        return chunks * (self.layers + 2)
+
     def predict(self, X, out, stream=None) -> None:
         s = C.c_void_p(stream.cuda_stream) if stream is not None else None
         N.check(self.L.blpg_mlp_predict(self.h, _vp(X), X.shape[0], _vp(out), s),
@@ -198,6 +204,11 @@ class WarmStart:
         return rep
 
     # ---- inference --------------------------------------------------------
+    def hint_launches(self, count: int) -> int:
+        """Kernels one predict_hint() over `count` LPs launches: features,
+        the network, top-m."""
+        return 1 + self.mlp.predict_launches((count + 63) // 64 * 64) + 1
+
     def predict_hint(self, d, m_dev, n_dev, offhint_dev, hint_out=None, stream=None,
                      scratch=None):
         """Basis hints (int32, packed m per LP) for a device batch."""
