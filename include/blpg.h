@@ -190,12 +190,19 @@ int32_t blpg_plan_num_classes(const blpg_plan* plan);
 int32_t blpg_plan_class_info(const blpg_plan* plan, int32_t cls,
                              int32_t* cluster, int32_t* threads,
                              int32_t* smem_bytes, int32_t* num_lps);
+/* Residency of size class `cls`: CTAs of it resident per SM and the
+ * persistent grid (CTAs) it is launched with. */
+int32_t blpg_plan_class_residency(const blpg_plan* plan, int32_t cls,
+                                  int32_t* ctas_per_sm, int32_t* grid);
 /* Kernel launches one blpg_plan_execute performs. */
 int32_t blpg_plan_launches(const blpg_plan* plan);
 void blpg_plan_destroy(blpg_plan* plan);
 
 /* Size-class table (JSON text, as written by the autotuner): overrides the
- * built-in heuristic for threads per CTA and cluster size.  Null resets. */
+ * built-in heuristic for threads per CTA ("fp64_k1": 256, per precision and
+ * cluster size), the per-CTA shared-memory budget ("fp32_smem": bytes) and
+ * the CTAs per SM target ("fp32_ctas": 2; default: as many as shared memory
+ * admits).  Null resets. */
 int32_t blpg_set_tuning(const char* json_text);
 
 const char* blpg_last_error(void);

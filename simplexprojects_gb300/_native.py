@@ -59,6 +59,7 @@ SIGNATURES = {
                                       C.POINTER(Result), C.c_void_p]),
     "blpg_plan_num_classes": (C.c_int32, [C.c_void_p]),
     "blpg_plan_class_info": (C.c_int32, [C.c_void_p, C.c_int32, i32p, i32p, i32p, i32p]),
+    "blpg_plan_class_residency": (C.c_int32, [C.c_void_p, C.c_int32, i32p, i32p]),
     "blpg_plan_launches": (C.c_int32, [C.c_void_p]),
     "blpg_plan_destroy": (None, [C.c_void_p]),
     "blpg_set_tuning": (C.c_int32, [C.c_char_p]),

@@ -77,7 +77,8 @@ static int device_check(int device, cudaDeviceProp* prop) {
 }
 
 struct ClassPlan {
-  int K = 1, nt = 128, max_m = 0, max_ldw = 0, max_na = 0, smem = 0;
+  int K = 1, nt = 128, max_m = 0, max_ldw = 0, max_na = 0, max_nv = 0, smem = 0;
+  int ctas_per_sm = 1;
   int count = 0, grid = 0, order_off = 0;
   double work = 0;
 };
@@ -105,6 +106,7 @@ struct blpg_plan {
   blpg::LpArgs graph_args{};
   int launches = 0;
   int sm_count = 0;
+  int smem_per_sm = 0, smem_reserved = 0, regs_per_sm = 0, threads_per_sm = 0;
 };
 
 namespace blpg {
@@ -170,23 +172,50 @@ static int occupancy(const ClassPlan& c, int* ctas_per_sm, int* clusters) {
 
 constexpr int kMaxThreads = 512;  // __launch_bounds__ of solve_kernel
 
-// Threads per CTA: whole vector lanes per row group, at least `floor_threads`
-// in total (several row groups for narrow tableaux), at most 1024.
-static int pick_threads(const Geom& g, int precision, int K, int override_nt) {
-  if (override_nt > 0) {
-    int nt = dev::round_up(std::max(override_nt, g.nl), 32);
+template <typename T>
+static int kernel_regs(bool cluster) {
+  cudaFuncAttributes fa{};
+  cudaError_t e = cluster ? cudaFuncGetAttributes(&fa, dev::solve_kernel<T, true>)
+                          : cudaFuncGetAttributes(&fa, dev::solve_kernel<T, false>);
+  return e == cudaSuccess && fa.numRegs > 0 ? fa.numRegs : 128;
+}
+
+static int tuning_value(int key0, int key1, int dflt) {
+  std::lock_guard<std::mutex> lk(g_tuning.mu);
+  auto it = g_tuning.threads.find({key0, key1});
+  return it != g_tuning.threads.end() ? it->second : dflt;
+}
+
+// Threads per CTA for a class whose widest member has nl vector lanes per
+// row and whose layout takes smem bytes: first the CTAs per SM (as many as
+// shared memory admits, or the tuning table's "fpXX_ctas" target), then the
+// most threads -- whole rows of lanes, at most the tuning table's threads
+// per CTA (default 512) -- whose registers keep that many CTAs resident.
+// Fewer CTAs per SM when a row of lanes does not fit otherwise.
+static int pick_threads(const blpg_plan* p, int nl, int smem, int regs, int K, int override_nt,
+                        int* ctas_out) {
+  const int by_smem = std::max(1, p->smem_per_sm / (smem + p->smem_reserved));
+  int target = tuning_value(p->precision * 16 + 14, 2, 0);
+  target = target > 0 ? std::min(target, by_smem) : by_smem;
+  const int regs_alloc = dev::round_up(std::max(regs, 1), 8);
+  if (override_nt > 0) {  // explicit threads per CTA: residency follows from it
+    *ctas_out = 0;
+    return std::min(dev::round_up(std::max(override_nt, nl), 32), kMaxThreads);
+  }
+  const int want = tuning_value(p->precision * 16 + K, 0, 512);
+  for (int ctas = target; ctas >= 1; --ctas) {
+    int cap = std::min(kMaxThreads, (p->regs_per_sm / ctas) / (regs_alloc * 32) * 32);
+    cap = std::min(cap, p->threads_per_sm / ctas / 32 * 32);
+    if (cap < nl && ctas > 1) continue;
+    cap = std::max(cap, dev::round_up(nl, 32));
+    int G = std::max(1, std::min(want, cap) / nl);
+    int nt = dev::round_up(G * nl, 32);
+    while (nt > cap && G > 1) nt = dev::round_up(--G * nl, 32);
+    *ctas_out = ctas;
     return std::min(nt, kMaxThreads);
   }
-  int floor_threads = 512;
-  {
-    std::lock_guard<std::mutex> lk(g_tuning.mu);
-    auto it = g_tuning.threads.find({precision * 16 + K, 0});
-    if (it != g_tuning.threads.end()) floor_threads = it->second;
-  }
-  int G = std::max(1, floor_threads / g.nl);
-  int nt = dev::round_up(G * g.nl, 32);
-  if (nt > kMaxThreads) nt = dev::round_up(g.nl, 32);
-  return std::min(nt, kMaxThreads);
+  *ctas_out = 1;
+  return std::min(dev::round_up(nl, 32), kMaxThreads);
 }
 
 // Size classes.  Every LP gets the smallest cluster size K whose per-CTA
@@ -210,7 +239,7 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
   budget = std::min(budget, max_smem);
   const int min_cluster = std::max(1, std::min(p->opt.min_cluster, max_cluster));
   struct Item {
-    int K, nl, ldw;
+    int K, nl, ldw, nv;
     double work;
   };
   std::vector<Item> items(p->count);
@@ -221,10 +250,11 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
       const int lim = pass == 0 ? budget : max_smem;
       for (int K = min_cluster; K <= max_cluster; K *= 2) {
         Geom g(m, n, na, K, V);
-        if (Layout(m, g.ldw, elem).total <= lim && g.nl <= kMaxThreads) {
+        const int nv = n + m + na;
+        if (Layout(m, g.ldw, nv, elem).total <= lim && g.nl <= kMaxThreads) {
           chosen = K;
-          items[k] = {K, g.nl, g.ldw,
-                      (double)(m + 1) * (double)(n + m + na + 1) * (double)(m + n)};
+          items[k] = {K, g.nl, g.ldw, nv,
+                      (double)(m + 1) * (double)(n + na + 1) * (double)(m + n)};
           break;
         }
       }
@@ -253,10 +283,12 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
         ClassPlan& c = parts[ci];
         const int mm = std::max(c.max_m, p->m[lp]);
         const int ll = std::max(c.max_ldw, items[lp].ldw);
-        const int lim = std::max(budget, Layout(p->m[lp], items[lp].ldw, elem).total);
-        if (Layout(mm, ll, elem).total <= std::min(lim, max_smem)) {
+        const int vv = std::max(c.max_nv, items[lp].nv);
+        const int lim = std::max(budget, Layout(p->m[lp], items[lp].ldw, items[lp].nv, elem).total);
+        if (Layout(mm, ll, vv, elem).total <= std::min(lim, max_smem)) {
           c.max_m = mm;
           c.max_ldw = ll;
+          c.max_nv = vv;
           c.max_na = std::max(c.max_na, p->na[lp]);
           c.work += items[lp].work;
           c.nt = std::max(c.nt, items[lp].nl);
@@ -269,6 +301,7 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
         c.K = kv.first;
         c.max_m = p->m[lp];
         c.max_ldw = items[lp].ldw;
+        c.max_nv = items[lp].nv;
         c.max_na = p->na[lp];
         c.work = items[lp].work;
         c.nt = items[lp].nl;
@@ -278,13 +311,11 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
     }
     for (size_t ci = 0; ci < parts.size(); ++ci) {
       ClassPlan c = parts[ci];
-      Geom gmax(c.max_m, 1, 0, 1, V);
-      (void)gmax;
-      // threads: every member's row of vector lanes at least once
-      Geom gl(0, 0, 0, 1, V);
-      gl.nl = c.nt;  // c.nt holds the widest member's lane count here
-      c.nt = pick_threads(gl, p->precision, c.K, p->opt.threads_per_cta);
-      c.smem = Layout(c.max_m, c.max_ldw, elem).total;
+      c.smem = Layout(c.max_m, c.max_ldw, c.max_nv, elem).total;
+      // threads: every member's row of vector lanes at least once (c.nt
+      // holds the widest member's lane count here)
+      c.nt = pick_threads(p, c.nt, c.smem, kernel_regs<T>(c.K > 1), c.K,
+                          p->opt.threads_per_cta, &c.ctas_per_sm);
       c.count = (int)members[ci].size();
       c.order_off = (int)p->order.size();
       p->order.insert(p->order.end(), members[ci].begin(), members[ci].end());
@@ -292,6 +323,7 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
       int rc = occupancy<T>(c, &per_sm, &clusters);
       if (rc) return rc;
       int slots = c.K == 1 ? per_sm * p->sm_count : clusters;
+      if (c.K == 1) c.ctas_per_sm = per_sm;
       if (slots <= 0)
         return fail(BLPG_ETOOBIG, "class K=%d nt=%d smem=%d cannot be resident", c.K,
                     c.nt, c.smem);
@@ -319,6 +351,7 @@ static int launch_one(blpg_plan* p, size_t ci, const LpArgs& args, cudaStream_t 
   ca.max_m = c.max_m;
   ca.max_ldw = c.max_ldw;
   ca.max_na = c.max_na;
+  ca.max_nv = c.max_nv;
   if (c.K == 1) {
     dev::solve_kernel<T, false><<<c.grid, c.nt, c.smem, s>>>(args, ca);
     CK(cudaGetLastError());
@@ -391,8 +424,9 @@ extern "C" int32_t blpg_set_tuning(const char* json) {
   std::lock_guard<std::mutex> lk(g_tuning.mu);
   g_tuning.threads.clear();
   if (!json) return BLPG_OK;
-  // Minimal reader for {"fp64_k1": 256, "fp32_k2": 512, "fp64_smem": 115712, ...}:
-  // threads per CTA per (precision, cluster size) and the CTA smem budget.
+  // Minimal reader for {"fp64_k1": 256, "fp32_k2": 512, "fp64_smem": 115712,
+  // "fp32_ctas": 2, ...}: threads per CTA per (precision, cluster size), the
+  // CTA smem budget and the CTAs per SM target.
   const char* s = json;
   while ((s = std::strchr(s, '"'))) {
     const char* e = std::strchr(s + 1, '"');
@@ -407,6 +441,8 @@ extern "C" int32_t blpg_set_tuning(const char* json) {
     if (prec >= 0 && val > 0 && val <= 1024) g_tuning.threads[{prec * 16 + K, 0}] = val;
     if (key == "fp64_smem" && val > 0) g_tuning.threads[{BLPG_FP64 * 16 + 15, 1}] = val;
     if (key == "fp32_smem" && val > 0) g_tuning.threads[{BLPG_FP32 * 16 + 15, 1}] = val;
+    if (key == "fp64_ctas" && val > 0) g_tuning.threads[{BLPG_FP64 * 16 + 14, 2}] = val;
+    if (key == "fp32_ctas" && val > 0) g_tuning.threads[{BLPG_FP32 * 16 + 14, 2}] = val;
     s = colon + 1;
   }
   return BLPG_OK;
@@ -436,6 +472,10 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
   p->precision = opt.precision;
   p->count = bt->count;
   p->sm_count = prop.multiProcessorCount;
+  p->smem_per_sm = (int)prop.sharedMemPerMultiprocessor;
+  p->smem_reserved = (int)prop.reservedSharedMemPerBlock;
+  p->regs_per_sm = prop.regsPerMultiprocessor;
+  p->threads_per_sm = prop.maxThreadsPerMultiProcessor;
   const int N = bt->count;
   p->m.assign(bt->m, bt->m + N);
   p->n.assign(bt->n, bt->n + N);
@@ -623,6 +663,16 @@ extern "C" int32_t blpg_plan_class_info(const blpg_plan* p, int32_t cls, int32_t
   if (threads) *threads = c.nt;
   if (smem_bytes) *smem_bytes = c.smem;
   if (num_lps) *num_lps = c.count;
+  return BLPG_OK;
+}
+
+extern "C" int32_t blpg_plan_class_residency(const blpg_plan* p, int32_t cls,
+                                             int32_t* ctas_per_sm, int32_t* grid) {
+  if (!p || cls < 0 || cls >= (int32_t)p->classes.size())
+    return fail(BLPG_EINVAL, "blpg_plan_class_residency: bad plan or class");
+  const ClassPlan& c = p->classes[cls];
+  if (ctas_per_sm) *ctas_per_sm = c.ctas_per_sm;
+  if (grid) *grid = c.grid;
   return BLPG_OK;
 }
 

@@ -7,6 +7,16 @@
 //
 // Reference kernel: BLPG-Solver/src/simplex.cu:35-385 (mykernel).  Same
 // method, rebuilt for Blackwell:
+//   - the tableau is condensed: basic columns are unit vectors, so only the
+//     nonbasic columns and the RHS are stored, (m + 1) x (n + na + 1)
+//     instead of (m + 1) x (n + m + na + 1).  A pivot on (r, q) puts the
+//     leaving variable into q's column slot with entries 1/a_rq in row r and
+//     -t_iq / a_rq elsewhere, which are the values the full tableau's
+//     elimination writes into that variable's unit column; slot labels
+//     (cvar) and variable positions (vpos) are kept beside the tableau, and
+//     ties are broken on variable ids, so every decision and every output
+//     matches the full-tableau oracle (only signs of zero entries inside the
+//     tableau may differ, and a zero never decides anything);
 //   - the whole tableau lives in shared memory (the reference keeps it in
 //     global memory and reduces through global scratch, simplex.cu:108-143);
 //   - pricing and the ratio test are warp argmins with __reduce_min_sync on
@@ -88,6 +98,7 @@ struct ClassArgs {
   int32_t max_m;    // smem layout is sized for these
   int32_t max_ldw;
   int32_t max_na;   // artificial columns (two-phase LPs)
+  int32_t max_nv;   // variables n + m + na
 };
 
 template <typename T>
@@ -106,17 +117,18 @@ struct VecT<float> {
 __host__ __device__ inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
 __host__ __device__ inline int round_up(int a, int b) { return ceil_div(a, b) * b; }
 
-// Per-LP column geometry.  Columns 0..n-1 structural, n..n+m-1 slacks,
-// n+m..n+m+na-1 artificials (two-phase only); CTA k of the cluster holds
-// global columns [k*cw, k*cw + cw) at local 0..cw-1, the RHS at local cw,
-// zero padding after it; rows 0..m-1 constraints, row m objective.
+// Per-LP column geometry.  Variables 0..n-1 structural, n..n+m-1 slacks,
+// n+m..n+m+na-1 artificials (two-phase only).  The tableau stores Wc = n + na
+// column slots (one per nonbasic variable); CTA k of the cluster holds slots
+// [k*cw, k*cw + cw) at local 0..cw-1, the RHS at local cw, zero padding after
+// it; rows 0..m-1 constraints, row m objective.
 struct Geom {
   int m, n, na, Wc, cw, ldw, nl;
   __host__ __device__ Geom(int m_, int n_, int na_, int K, int V) {
     m = m_;
     n = n_;
     na = na_;
-    Wc = n + m + na;
+    Wc = n + na;
     cw = round_up(ceil_div(Wc, K), V);
     ldw = cw + V;
     nl = ldw / V;
@@ -125,9 +137,10 @@ struct Geom {
 
 // Shared-memory layout of a class (bytes).  Identical on host and device.
 struct Layout {
-  int tab, colA, colB, rhsx, basis, flags, ext, red, state, total;
-  __host__ __device__ Layout(int max_m, int max_ldw, int elem) {
+  int tab, colA, colB, rhsx, basis, flags, cvar, vpos, ext, red, state, total;
+  __host__ __device__ Layout(int max_m, int max_ldw, int max_nv, int elem) {
     int mp1 = round_up(max_m + 1, 4);
+    int nvp = round_up(max_nv, 4);
     tab = 0;
     int off = round_up((max_m + 1) * max_ldw * elem, 16);
     colA = off;
@@ -140,6 +153,10 @@ struct Layout {
     off += round_up(mp1 * 4, 16);
     flags = off;
     off += round_up(mp1 * 4, 16);
+    cvar = off;  // variable id of every column slot
+    off += nvp * 4;
+    vpos = off;  // slot of every nonbasic variable, -1 - row of a basic one
+    off += nvp * 4;
     ext = off;
     if (elem == 4) off += 2 * mp1 * 8;  // FP64 x_B and duals of the refresh
     red = off;
@@ -192,19 +209,20 @@ __device__ __forceinline__ Key block_min(const Key& k, Key* red) {
   return warp_min(v);
 }
 
-// Pricing key of reduced cost d at global column j (only d < -tol is
-// eligible).  For negative numbers ~bits is increasing in the value, so the
-// most negative d has the smallest key; Bland's rule zeroes the value words
-// so the lowest index wins.
-__device__ __forceinline__ Key price_key(double d, int j, bool bland) {
+// Pricing key of reduced cost d of variable j in column slot s (only
+// d < -tol is eligible).  For negative numbers ~bits is increasing in the
+// value, so the most negative d has the smallest key; ties go to the lowest
+// variable id; Bland's rule zeroes the value words so the lowest variable id
+// wins.  The payload is the slot.
+__device__ __forceinline__ Key price_key(double d, int j, int s, bool bland) {
   unsigned long long u = ~(unsigned long long)__double_as_longlong(d);
   if (bland) u = 0ull;
-  return Key{(unsigned)(u >> 32), (unsigned)u, (unsigned)j, 0u};
+  return Key{(unsigned)(u >> 32), (unsigned)u, (unsigned)j, (unsigned)s};
 }
-__device__ __forceinline__ Key price_key(float d, int j, bool bland) {
+__device__ __forceinline__ Key price_key(float d, int j, int s, bool bland) {
   unsigned u = ~__float_as_uint(d);
   if (bland) u = 0u;
-  return Key{u, 0u, (unsigned)j, 0u};
+  return Key{u, 0u, (unsigned)j, (unsigned)s};
 }
 // Ratio key of theta >= 0 (IEEE bits are increasing for non-negative values),
 // ties by lowest basic-variable id, payload = row.
@@ -247,6 +265,21 @@ __device__ __forceinline__ double vget<double2, double>(const double2& v, int e)
 template <>
 __device__ __forceinline__ float vget<float4, float>(const float4& v, int e) {
   return e == 0 ? v.x : (e == 1 ? v.y : (e == 2 ? v.z : v.w));
+}
+
+__device__ __forceinline__ double sdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float sdiv(float a, float b) { return __fdiv_rn(a, b); }
+// Local index of global slot s on the CTA holding slots [c0, c0 + cw), -1 on
+// the other CTAs.
+__device__ __forceinline__ int local_slot(int s, int c0, int cw) {
+  return s >= c0 && s < c0 + cw ? s - c0 : -1;
+}
+
+__device__ __forceinline__ void vset(double2& v, int e, double x) {
+  if (e == 0) v.x = x; else v.y = x;
+}
+__device__ __forceinline__ void vset(float4& v, int e, float x) {
+  if (e == 0) v.x = x; else if (e == 1) v.y = x; else if (e == 2) v.z = x; else v.w = x;
 }
 
 __device__ __forceinline__ double2 v_fma(double f, const double2& p, const double2& t) {
@@ -297,6 +330,8 @@ struct Solver {
   T* rhsx;
   int* basis;
   int* flags;
+  int* cvar;   // slot -> variable id (every slot of the LP, replicated per CTA)
+  int* vpos;   // variable -> slot if nonbasic, -1 - row if basic
   double* xr;  // FP32 tableau only: FP64 x_B of the refresh
   double* yr;  // FP32 tableau only: FP64 duals of the refresh
   Key* redP;
@@ -334,15 +369,16 @@ struct Solver {
   }
 
   // Local pricing over the objective row (no update): block + cluster min.
+  // Variables below price_cols are eligible.
   __device__ Key price_only(const Geom& g, int c0, int lc, bool bland, T opt_tol,
                             int price_cols) {
     Key k = key_none();
     const T* d = tab + (size_t)g.m * g.ldw;
     for (int lj = threadIdx.x; lj < lc; lj += blockDim.x) {
-      const int j = c0 + lj;
+      const int j = cvar[c0 + lj];
       const T v = d[lj];
       if (j < price_cols && v < -opt_tol) {
-        Key kk = price_key(v, j, bland);
+        Key kk = price_key(v, j, c0 + lj, bland);
         if (key_less(kk, k)) k = kk;
       }
     }
@@ -350,10 +386,10 @@ struct Solver {
     return cluster_min(k);
   }
 
-  // Owner of column q copies it (rows 0..m) and the RHS column into the
-  // extraction buffers.
-  __device__ void extract(const Geom& g, int q, int c0, T* colx) {
-    const int ql = q - c0;
+  // Owner of slot s copies its column (rows 0..m) and the RHS column into
+  // the extraction buffers.
+  __device__ void extract(const Geom& g, int s, int c0, T* colx) {
+    const int ql = s - c0;
     for (int i = threadIdx.x; i <= g.m; i += blockDim.x) {
       colx[i] = tab[(size_t)i * g.ldw + ql];
       rhsx[i] = tab[(size_t)i * g.ldw + g.cw];
@@ -415,20 +451,29 @@ struct Solver {
     return k2;
   }
 
-  // Pivot row scale + objective-row update + pricing of the next column.
-  __device__ Key pivot_rows(const Geom& g, int r, const T* pcol, int c0, int lc,
-                            bool bland, T opt_tol, int price_cols) {
+  // Pivot on (r, slot s): the pivot row is divided by the pivot and its slot
+  // s entry becomes 1/pivot (the leaving variable's column), the objective
+  // row is updated with its slot s entry taken as 0 (the leaving variable's
+  // reduced cost before the pivot), and the next column is priced; lv is the
+  // leaving variable, now the label of slot s.
+  __device__ Key pivot_rows(const Geom& g, int r, int s, int lv, const T* pcol, int c0,
+                            int lc, bool bland, T opt_tol, int price_cols) {
     const T piv = pcol[r];
     const T dq = pcol[g.m];
+    const T rcp = sdiv(T(1), piv);
     T* prow = tab + (size_t)r * g.ldw;
     T* drow = tab + (size_t)g.m * g.ldw;
+    const int sl = local_slot(s, c0, g.cw);
     Key k = key_none();
     for (int v = threadIdx.x; v < g.nl; v += blockDim.x) {
+      const bool has_s = sl >= v * V && sl < v * V + V;
       VT p = *reinterpret_cast<const VT*>(prow + v * V);
       p = v_div(p, piv);
+      if (has_s) vset(p, sl - v * V, rcp);
       *reinterpret_cast<VT*>(prow + v * V) = p;
       VT d = *reinterpret_cast<const VT*>(drow + v * V);
       if (dq != T(0)) {
+        if (has_s) vset(d, sl - v * V, T(0));
         d = v_fma(dq, p, d);
         *reinterpret_cast<VT*>(drow + v * V) = d;
       }
@@ -436,10 +481,12 @@ struct Solver {
       for (int e = 0; e < V; ++e) {
         const int lj = v * V + e;
         const T dv = vget<VT, T>(d, e);
-        const int j = c0 + lj;
-        if (lj < lc && j < price_cols && dv < -opt_tol) {
-          Key kk = price_key(dv, j, bland);
-          if (key_less(kk, k)) k = kk;
+        if (lj < lc && dv < -opt_tol) {
+          const int j = lj == sl ? lv : cvar[c0 + lj];
+          if (j < price_cols) {
+            Key kk = price_key(dv, j, c0 + lj, bland);
+            if (key_less(kk, k)) k = kk;
+          }
         }
       }
     }
@@ -447,20 +494,34 @@ struct Solver {
     return cluster_min(k);
   }
 
-  // Rank-1 update of rows 0..m-1 except r; the owner of the next column qn
-  // extracts it into colx_next, every CTA extracts its RHS replica.
-  __device__ void update_body(const Geom& g, int r, const T* pcol, int qn, int owner_n, int c0,
-                              T* colx_next) {
-    update_rows(tab, rhsx, rank, g.m, g.ldw, g.nl, g.cw, r, pcol, qn, owner_n, c0, colx_next);
+  // Labels after a pivot on (r, slot s) that brought q in for lv (one
+  // thread; every CTA of a cluster updates its own replica).
+  __device__ void relabel(int r, int s, int q, int lv) {
+    if (threadIdx.x == 0) {
+      basis[r] = q;
+      cvar[s] = lv;
+      vpos[lv] = s;
+      vpos[q] = -1 - r;
+    }
+  }
+
+  // Rank-1 update of rows 0..m-1 except r; the owner of the next slot sn
+  // extracts its column into colx_next, every CTA extracts its RHS replica.
+  __device__ void update_body(const Geom& g, int r, int s, const T* pcol, int sn, int owner_n,
+                              int c0, T* colx_next) {
+    update_rows(tab, rhsx, rank, g.m, g.ldw, g.nl, g.cw, r, s, pcol, sn, owner_n, c0,
+                colx_next);
   }
   // Kept out of line with plain arguments (no `this`, no structs by
   // reference) so that the unrolled sweep has its own register budget and
-  // nothing in its loop lives in local memory.
+  // nothing in its loop lives in local memory.  The slot s entry of every
+  // updated row is taken as 0 before the elimination (it held the entering
+  // column, whose slot now carries the leaving variable's unit column).
   static __device__ __noinline__ void update_rows(T* const tb, T* const rhsx, const int rank,
                                                   const int m, const int ldw, const int nl,
-                                                  const int cw, const int r, const T* pcol,
-                                                  const int qn, const int owner_n, const int c0,
-                                                  T* colx_next) {
+                                                  const int cw, const int r, const int s,
+                                                  const T* pcol, const int qn, const int owner_n,
+                                                  const int c0, T* colx_next) {
     const int nt = (int)blockDim.x;
     const int G = nt / nl;
     const int grp = threadIdx.x / nl;
@@ -471,6 +532,9 @@ struct Solver {
     const bool has_q = qn >= 0 && owner_n == rank && (qloc / V) == lane;
     const int qe = qloc - lane * V;
     const bool has_rhs = lane == cw / V;
+    const int sl = local_slot(s, c0, cw);
+    const bool has_s = sl >= lane * V && sl < lane * V + V;
+    const int se = sl - lane * V;
     // kU rows per step, every load issued before any store (rows
     // grp, grp + G, ... are disjoint, so this only adds memory parallelism)
     constexpr int kU = 1;  // measured: deeper unrolling of the sweep is slower
@@ -492,6 +556,7 @@ struct Solver {
           if (i == r) {
             t[u] = p;
           } else if (f[u] != T(0)) {  // a zero multiplier leaves the row as it is
+            if (has_s) vset(t[u], se, T(0));
             t[u] = v_fma(f[u], p, t[u]);
             *reinterpret_cast<VT*>(tb + (size_t)i * ldw + lane * V) = t[u];
           }
@@ -511,11 +576,12 @@ struct Solver {
     const T opt_tol = (T)a.opt_tol, piv_tol = (T)a.piv_tol, feas_tol = (T)a.feas_tol;
     const T deg_tol = (T)a.deg_tol;
     Key kq = price_only(g, c0, lc, bland, opt_tol, price_cols);
-    int q = kq.w2 == ~0u ? -1 : (int)kq.w2;
+    int q = kq.w2 == ~0u ? -1 : (int)kq.w2;  // entering variable
     if (q < 0) return kOpt;
     if (pivots >= max_piv) return kUndef;
-    int owner = q / g.cw;
-    if (owner == rank) extract(g, q, c0, colbuf(cur));
+    int s = (int)kq.w3;  // its slot
+    int owner = s / g.cw;
+    if (owner == rank) extract(g, s, c0, colbuf(cur));
     __syncthreads();
     for (;;) {
       // A: ratio test on the owner of q
@@ -554,12 +620,14 @@ struct Solver {
       }
       // C: pivot row, objective row, next pricing (cluster barrier B2 inside)
       const T* pcol = colbuf(cur);
-      Key kn = pivot_rows(g, r, pcol, c0, lc, bland, opt_tol, price_cols);
+      const int lv = basis[r];
+      Key kn = pivot_rows(g, r, s, lv, pcol, c0, lc, bland, opt_tol, price_cols);
       const int qn = kn.w2 == ~0u ? -1 : (int)kn.w2;
-      const int owner_n = qn >= 0 ? qn / g.cw : -1;
-      if (threadIdx.x == 0) basis[r] = q;
+      const int sn = qn >= 0 ? (int)kn.w3 : -1;
+      const int owner_n = qn >= 0 ? sn / g.cw : -1;
+      relabel(r, s, q, lv);
       // D: body update, extraction of the next pivot column
-      update_body(g, r, pcol, qn, owner_n, c0, colbuf(cur ^ 1));
+      update_body(g, r, s, pcol, sn, owner_n, c0, colbuf(cur ^ 1));
       __syncthreads();
       cur ^= 1;
       ++pivots;
@@ -567,12 +635,13 @@ struct Solver {
       if (pivots >= max_piv) return kUndef;
       if (period > 0 && pivots % period == 0) return kRefresh;
       q = qn;
+      s = sn;
       owner = owner_n;
     }
   }
 
   // Objective row from the current basis: d_j = sum_i cB_i T_ij - c_j over
-  // local columns (phase II after phase I), or the phase I row
+  // local slots (phase II after phase I), or the phase I row
   // -sum_{artificial rows} T_ij.  Sums run over rows in increasing order, as
   // the oracle does.
   __device__ void objective_row(const Geom& g, int c0, int lc, const double* c,
@@ -581,10 +650,13 @@ struct Solver {
     for (int lj = threadIdx.x; lj <= g.cw; lj += blockDim.x) {
       const bool is_rhs = lj == g.cw;
       if (!is_rhs && lj >= lc) continue;
-      const int j = is_rhs ? -1 : c0 + lj;
+      const int j = is_rhs ? -1 : cvar[c0 + lj];
       T acc = T(0);
       if (phase1) {
-        if (!is_rhs && j >= nart0) continue;  // artificial: stays 0
+        if (!is_rhs && j >= nart0) {  // artificial: stays 0
+          tab[(size_t)g.m * g.ldw + lj] = T(0);
+          continue;
+        }
         for (int i = 0; i < g.m; ++i)
           if (basis[i] >= nart0) acc = acc - tab[(size_t)i * g.ldw + lj];
         tab[(size_t)g.m * g.ldw + lj] = acc;
@@ -603,7 +675,7 @@ struct Solver {
   __device__ static float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 
   // Drive zero-level artificials out of the basis after phase I: for each
-  // such row, pivot on the lowest column j < n+m with |T_ij| > piv_tol.
+  // such row, pivot on the lowest variable j < n+m with |T_ij| > piv_tol.
   __device__ void drive_out(const Geom& g, int c0, int lc, const LpArgs& a, int& pivots,
                             int& cur) {
     const T piv_tol = (T)a.piv_tol;
@@ -613,10 +685,10 @@ struct Solver {
       Key k = key_none();
       const T* row = tab + (size_t)i * g.ldw;
       for (int lj = threadIdx.x; lj < lc; lj += blockDim.x) {
-        const int j = c0 + lj;
+        const int j = cvar[c0 + lj];
         const T v = row[lj];
         if (j < nart0 && (v > piv_tol || v < -piv_tol)) {
-          Key kk{0u, 0u, (unsigned)j, 0u};
+          Key kk{0u, 0u, (unsigned)j, (unsigned)(c0 + lj)};
           if (key_less(kk, k)) k = kk;
         }
       }
@@ -624,17 +696,17 @@ struct Solver {
       k = cluster_min(k);
       if (CLUSTER) csync();  // pslot reads done before the next write
       if (k.w2 == ~0u) continue;  // redundant row: artificial stays basic at 0
-      pivot_on(g, i, (int)k.w2, c0, lc, cur);
+      pivot_on(g, i, (int)k.w2, (int)k.w3, c0, lc, cur);
       ++pivots;
     }
   }
 
-  // Pivot on (r, q) without pricing (phase-I drive-out, warm-start crash,
-  // dual simplex).  Column q is extracted by its owner and copied by the
-  // other CTAs of the cluster; returns with every copy done.
-  __device__ void pivot_on(const Geom& g, int r, int q, int c0, int lc, int cur) {
-    const int owner = q / g.cw;
-    if (owner == rank) extract(g, q, c0, colbuf(cur));
+  // Pivot on (r, q in slot s) without pricing (phase-I drive-out, warm-start
+  // crash, dual simplex).  The column is extracted by its owner and copied by
+  // the other CTAs of the cluster; returns with every copy done.
+  __device__ void pivot_on(const Geom& g, int r, int q, int s, int c0, int lc, int cur) {
+    const int owner = s / g.cw;
+    if (owner == rank) extract(g, s, c0, colbuf(cur));
     if (CLUSTER) {
       csync();
       if (owner != rank) {
@@ -644,9 +716,10 @@ struct Solver {
     }
     __syncthreads();
     const T* pcol = colbuf(cur);
-    pivot_rows(g, r, pcol, c0, lc, false, T(0), 0);
-    if (threadIdx.x == 0) basis[r] = q;
-    update_body(g, r, pcol, -1, -1, c0, colbuf(cur ^ 1));
+    const int lv = basis[r];
+    pivot_rows(g, r, s, lv, pcol, c0, lc, false, T(0), 0);
+    relabel(r, s, q, lv);
+    update_body(g, r, s, pcol, -1, -1, c0, colbuf(cur ^ 1));
     __syncthreads();
     if (CLUSTER) csync();
   }
@@ -671,7 +744,7 @@ struct Solver {
       badp = badp || tab[(size_t)i * g.ldw + g.cw] < -ptol;
     const T* d = tab + (size_t)g.m * g.ldw;
     for (int lj = threadIdx.x; lj < lc; lj += blockDim.x)
-      badd = badd || (c0 + lj < g.n + g.m && d[lj] < -opt_tol);
+      badd = badd || (cvar[c0 + lj] < g.n + g.m && d[lj] < -opt_tol);
     badp = __syncthreads_or(badp ? 1 : 0) != 0;  // RHS is replicated: no exchange
     badd = cluster_any(badd);
     return (badp ? 0 : 1) | (badd ? 0 : 2);
@@ -680,7 +753,7 @@ struct Solver {
   // Dual simplex from a dual-feasible basis (the oracle's dual_loop):
   // leaving row = most negative RHS below -ptol (ties lowest basic
   // variable); entering column = minimum max(d_j, 0) / -T_rj over
-  // T_rj < -piv_tol (ties lowest column).  kOpt once x_B >= -ptol; kNoFeas
+  // T_rj < -piv_tol (ties lowest variable).  kOpt once x_B >= -ptol; kNoFeas
   // when no column can enter (the LP would be primal infeasible).
   __device__ int dual_loop(const Geom& g, int c0, int lc, const LpArgs& a, int max_piv,
                            int& pivots, int cur, T ptol) {
@@ -703,16 +776,16 @@ struct Solver {
       const T dual_tol = (T)a.opt_tol;
       // Harris (as the primal test): pass 1 bounds the dual step by the
       // ratios relaxed by opt_tol, pass 2 takes the largest |T_rj| within it
-      // (ties lowest column).  Textbook rule when Harris is off.
+      // (ties lowest variable).  Textbook rule when Harris is off.
       Key kq = key_none();
       for (int lj = threadIdx.x; lj < lc; lj += blockDim.x) {
-        const int j = c0 + lj;
+        const int j = cvar[c0 + lj];
         const T arj = row[lj];
         if (j < g.n + g.m && arj < -piv_tol) {
           const T dj = drow[lj];
           const T th = a.harris ? ((dj > T(0) ? dj : T(0)) + dual_tol) / (-arj)
                                 : (dj > T(0) ? dj / (-arj) : T(0));
-          Key kk = ratio_key(th, j, 0);
+          Key kk = ratio_key(th, j, c0 + lj);
           if (key_less(kk, kq)) kq = kk;
         }
       }
@@ -724,13 +797,13 @@ struct Solver {
         const T tmax = key_theta(kq, T(0));
         Key k2 = key_none();
         for (int lj = threadIdx.x; lj < lc; lj += blockDim.x) {
-          const int j = c0 + lj;
+          const int j = cvar[c0 + lj];
           const T arj = row[lj];
           if (j < g.n + g.m && arj < -piv_tol) {
             const T dj = drow[lj];
             const T th = dj > T(0) ? dj / (-arj) : T(0);
             if (th <= tmax) {
-              Key kk = big_key(-arj, j, 0);
+              Key kk = big_key(-arj, j, c0 + lj);
               if (key_less(kk, k2)) k2 = kk;
             }
           }
@@ -739,7 +812,7 @@ struct Solver {
         kq = cluster_min(k2);
         if (CLUSTER) csync();
       }
-      pivot_on(g, r, (int)kq.w2, c0, lc, cur);
+      pivot_on(g, r, (int)kq.w2, (int)kq.w3, c0, lc, cur);
       ++pivots;
     }
   }
@@ -762,14 +835,13 @@ struct Solver {
     for (int k = 0; k < g.m; ++k) {
       const int h = hint[k];
       if (h < 0 || h >= g.n) continue;
-      bool isbasic = false;
-      for (int i = threadIdx.x; i < g.m; i += blockDim.x) isbasic = isbasic || basis[i] == h;
-      if (__syncthreads_or(isbasic ? 1 : 0)) continue;  // duplicate hint entry
-      const int owner = h / g.cw;
+      const int s = vpos[h];
+      if (s < 0) continue;  // already basic (duplicate hint entry)
+      const int owner = s / g.cw;
       int r = -1;
       if (owner == rank) {
         Key kk = key_none();
-        const int hl = h - c0;
+        const int hl = s - c0;
         for (int i = threadIdx.x; i < g.m; i += blockDim.x) {
           const int bi = basis[i];
           if (bi >= g.n && bi < g.n + g.m && !flags[bi - g.n]) {
@@ -791,21 +863,29 @@ struct Solver {
         csync();
       }
       if (r < 0) {
+        __syncthreads();  // redR is read again by the next column's search
         ++missing;
         continue;
       }
-      pivot_on(g, r, h, c0, lc, cur);
+      pivot_on(g, r, h, s, c0, lc, cur);
       ++pivots;
     }
     return missing;
   }
 
-  // Tableau element (row i, global column j) wherever it lives.
-  __device__ T* elem(const Geom& g, int i, int j) {
-    if (!CLUSTER) return tab + (size_t)i * g.ldw + j;
-    const int o = j / g.cw;
-    T* p = tab + (size_t)i * g.ldw + (j - o * g.cw);
+  // Tableau element (row i, global slot s) wherever it lives.
+  __device__ T* elem(const Geom& g, int i, int s) {
+    if (!CLUSTER) return tab + (size_t)i * g.ldw + s;
+    const int o = s / g.cw;
+    T* p = tab + (size_t)i * g.ldw + (s - o * g.cw);
     return o == rank ? p : remote(p, o);
+  }
+  // Element (i, k) of B^-1 = column of slack k: a stored column when the
+  // slack is nonbasic, the unit vector of its row when it is basic.
+  __device__ T binv(const Geom& g, int i, int k) {
+    const int v = vpos[g.n + k];
+    if (v >= 0) return *elem(g, i, v);
+    return i == -1 - v ? T(1) : T(0);
   }
 
   // FP64 refresh of the FP32 tableau: x_B and the duals y are recomputed
@@ -825,22 +905,18 @@ struct Solver {
     int ok = 0;
     if (rank == 0) {
       double* res = reinterpret_cast<double*>(col0);  // col0|col1: m doubles
-      // Structural basics as a compact list (row, column); for every slack
-      // the row where it is basic (-1 when nonbasic).  flags[] holds the
-      // list (its warm-start use is over by now), slackrow aliases yr until
-      // the duals are needed.
+      // Structural basics as a compact list of rows, in row order; flags[]
+      // holds it (its warm-start use is over by now).  The row where slack k
+      // is basic is -1 - vpos[n + k] (vpos[n + k] < 0).
       int* slist = flags;
-      int* slackrow = reinterpret_cast<int*>(yr);
       int* wcount = reinterpret_cast<int*>(redH);  // per-32-row chunk counts (<= 128)
       const int nchunks = ceil_div(m, 32);
-      for (int k = tid; k < m; k += nt) slackrow[k] = -1;
       // row-ordered compaction: ballot per 32-row chunk, then a prefix sum
       for (int ch = warp; ch < nchunks; ch += nw) {
         const int i = ch * 32 + lane;
         const bool st = i < m && basis[i] < n;
         const unsigned bal = __ballot_sync(0xffffffffu, st);
         if (lane == 0) wcount[ch] = __popc(bal);
-        if (i < m && !st && basis[i] < n + m) slackrow[basis[i] - n] = i;
       }
       __syncthreads();
       if (tid == 0) {
@@ -889,8 +965,8 @@ struct Solver {
           const double sum = (q & 2) ? p2 + s01 : s01 + p2;
           if (k < m && q == 0) {
             double r = b[k] - sum;
-            const int sr = slackrow[k];
-            if (sr >= 0) r = r - xr[sr];
+            const int sv = vpos[n + k];
+            if (sv < 0) r = r - xr[-1 - sv];
             res[k] = r;
           }
         }
@@ -898,7 +974,7 @@ struct Solver {
         for (int i = warp; i < m; i += nw) {
           float acc = 0.f;
           for (int k = lane; k < m; k += 32)
-            acc = fmaf((float)*elem(g, i, n + k), (float)res[k], acc);
+            acc = fmaf((float)binv(g, i, k), (float)res[k], acc);
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
           if (lane == 0) {
@@ -911,8 +987,12 @@ struct Solver {
         if (__uint_as_float(mx[0]) <= 1e-10f * fmaxf(1.f, __uint_as_float(mx[1]))) break;
         __syncthreads();
       }
-      __syncthreads();  // slackrow (aliasing yr) no longer needed
-      for (int k = tid; k < m; k += nt) yr[k] = (double)*elem(g, m, n + k);
+      __syncthreads();
+      // initial duals: y_k = d of slack k (0 when the slack is basic)
+      for (int k = tid; k < m; k += nt) {
+        const int sv = vpos[n + k];
+        yr[k] = sv >= 0 ? (double)*elem(g, m, sv) : 0.0;
+      }
       for (int it = 0; it < 2; ++it) {
         if (tid == 0) mx[0] = mx[1] = 0u;
         __syncthreads();
@@ -941,9 +1021,16 @@ struct Solver {
         for (int w = tid; w < H * m; w += nt) {
           const int k = w % m, h = w / m;
           const int i0 = h * mh, i1 = min(m, i0 + mh);
+          const int sv = vpos[n + k];
           float acc = 0.f;
+          if (sv >= 0) {
 #pragma unroll 4
-          for (int i = i0; i < i1; ++i) acc = fmaf((float)res[i], (float)*elem(g, i, n + k), acc);
+            for (int i = i0; i < i1; ++i) acc = fmaf((float)res[i], (float)*elem(g, i, sv), acc);
+          } else {
+            // basic slack: column k of B^-1 is the unit vector of its row
+            const int row = -1 - sv;
+            if (row >= i0 && row < i1) acc = (float)res[row];
+          }
           if (H == 2) {
             half[h * m + k] = acc;
           } else {
@@ -982,13 +1069,15 @@ struct Solver {
         const double sum = (q & 2) ? p2 + s01 : s01 + p2;
         if (j < n && q == 0) {
           const double d = sum - c[j];
-          *elem(g, m, j) = (T)d;
+          const int sv = vpos[j];
+          if (sv >= 0) *elem(g, m, sv) = (T)d;
           badd = badd || d < -a.opt_tol;
         }
       }
       for (int k = tid; k < m; k += nt) {
         const double d = yr[k];
-        *elem(g, m, n + k) = (T)d;
+        const int sv = vpos[n + k];
+        if (sv >= 0) *elem(g, m, sv) = (T)d;
         badd = badd || d < -a.opt_tol;
       }
       for (int i = tid; i < m; i += nt) {
@@ -1024,39 +1113,79 @@ struct Solver {
     return ok;
   }
 
-  // Build the slack-basis tableau of LP lp (rows with b_i < 0 negated, with
-  // an artificial column each); coalesced along rows of A.
+  // Build the slack-basis tableau of LP lp: rows with b_i < 0 are negated
+  // and get an artificial variable each (the a-th such row's artificial is
+  // basic there and its slack takes column slot n + a); structural j sits in
+  // slot j.  Coalesced along rows of A.
   __device__ void load(const Geom& g, int c0, int lc, const double* A, const double* b,
                        const double* c) {
     const int tid = threadIdx.x, nt = blockDim.x;
     const int m = g.m, n = g.n, na = g.na;
     const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
-    for (int i = warp; i <= m; i += nw) {
-      const bool neg = i < m && b[i] < 0.0;
-      const T sgn = neg ? T(-1) : T(1);
-      int aidx = -1;
-      if (neg && na > 0) {
-        int cnt = 0;
-        for (int i2 = lane; i2 < i; i2 += 32) cnt += b[i2] < 0.0 ? 1 : 0;
-        cnt = __reduce_add_sync(0xffffffffu, cnt);
-        aidx = cnt;
+    if (na > 0) {
+      // flags[i] = index a of negated row i among the negated rows, else -1
+      // (ballot per 32-row chunk, then a prefix sum over the chunks)
+      int* wcount = reinterpret_cast<int*>(redH);
+      const int nchunks = ceil_div(m, 32);
+      for (int ch = warp; ch < nchunks; ch += nw) {
+        const int i = ch * 32 + lane;
+        const unsigned bal = __ballot_sync(0xffffffffu, i < m && b[i] < 0.0);
+        if (lane == 0) wcount[ch] = __popc(bal);
       }
+      __syncthreads();
+      if (tid == 0) {
+        int acc = 0;
+        for (int ch = 0; ch < nchunks; ++ch) {
+          const int v = wcount[ch];
+          wcount[ch] = acc;
+          acc += v;
+        }
+      }
+      __syncthreads();
+      for (int ch = warp; ch < nchunks; ch += nw) {
+        const int i = ch * 32 + lane;
+        const bool neg = i < m && b[i] < 0.0;
+        const unsigned bal = __ballot_sync(0xffffffffu, neg);
+        if (i < m) flags[i] = neg ? wcount[ch] + __popc(bal & ((1u << lane) - 1u)) : -1;
+      }
+      __syncthreads();
+    }
+    // labels
+    for (int v = tid; v < n + m; v += nt) {
+      if (v < n) {
+        cvar[v] = v;
+        vpos[v] = v;
+      } else {
+        const int i = v - n;
+        const int ai = na > 0 ? flags[i] : -1;
+        if (ai >= 0) {
+          cvar[n + ai] = v;
+          vpos[v] = n + ai;
+          vpos[n + m + ai] = -1 - i;
+          basis[i] = n + m + ai;
+        } else {
+          vpos[v] = -1 - i;
+          basis[i] = v;
+        }
+      }
+    }
+    __syncthreads();
+    for (int i = warp; i <= m; i += nw) {
+      const bool neg = i < m && na > 0 && flags[i] >= 0;
       T* row = tab + (size_t)i * g.ldw;
       for (int lj = lane; lj < g.ldw; lj += 32) {
         T v = T(0);
         if (lj < lc) {
-          const int j = c0 + lj;
-          if (i < m) {
-            if (j < n) {
-              const T av = (T)A[(size_t)i * n + j];
+          const int s = c0 + lj;
+          if (s < n) {
+            if (i < m) {
+              const T av = (T)A[(size_t)i * n + s];
               v = neg ? -av : av;
-            } else if (j < n + m) {
-              v = (j - n == i) ? sgn : T(0);
-            } else {
-              v = (aidx >= 0 && j - n - m == aidx) ? T(1) : T(0);
+            } else if (na == 0) {
+              v = -(T)c[s];
             }
-          } else if (na == 0 && j < n) {
-            v = -(T)c[j];
+          } else if (i < m && cvar[s] - n == i) {
+            v = T(-1);  // the negated row's slack
           }
         } else if (lj == g.cw && i < m) {
           const T bv = (T)b[i];
@@ -1064,7 +1193,6 @@ struct Solver {
         }
         row[lj] = v;
       }
-      if (i < m && lane == 0) basis[i] = neg ? n + m + aidx : n + i;
     }
     __syncthreads();
   }
@@ -1092,7 +1220,7 @@ struct Solver {
       for (int i = tid; i < m; i += nt) na += b[i] < 0.0 ? 1 : 0;
       na = block_sum(na);
       const Geom g(m, n, na, K, V);
-      if (m > ca.max_m || g.ldw > ca.max_ldw) {
+      if (m > ca.max_m || g.ldw > ca.max_ldw || na > ca.max_na || n + m + na > ca.max_nv) {
         // the LP does not fit the layout this plan was built for (e.g. a
         // plan made without b has no room for phase-I columns): refuse it
         if (rank == 0 && tid == 0) {
@@ -1157,7 +1285,7 @@ struct Solver {
             info |= kInfoDual | kInfoShift;
             T* drow = tab + (size_t)m * g.ldw;
             for (int lj = tid; lj < lc; lj += nt) {
-              const int j = c0 + lj;
+              const int j = cvar[c0 + lj];
               if (j < n + m && drow[lj] < -opt_tol)
                 drow[lj] = (T)a.shift * (T(1) + (T)((j * 7919) % 1000) / T(1000));
             }
@@ -1254,7 +1382,7 @@ template <typename T, bool CLUSTER>
 __global__ void __launch_bounds__(512, 1) solve_kernel(const LpArgs a, const ClassArgs ca) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Solver<T, CLUSTER> s;
-  const Layout L(ca.max_m, ca.max_ldw, (int)sizeof(T));
+  const Layout L(ca.max_m, ca.max_ldw, ca.max_nv, (int)sizeof(T));
   s.smem = smem_raw;
   s.tab = reinterpret_cast<T*>(smem_raw + L.tab);
   s.col0 = reinterpret_cast<T*>(smem_raw + L.colA);
@@ -1262,6 +1390,8 @@ __global__ void __launch_bounds__(512, 1) solve_kernel(const LpArgs a, const Cla
   s.rhsx = reinterpret_cast<T*>(smem_raw + L.rhsx);
   s.basis = reinterpret_cast<int*>(smem_raw + L.basis);
   s.flags = reinterpret_cast<int*>(smem_raw + L.flags);
+  s.cvar = reinterpret_cast<int*>(smem_raw + L.cvar);
+  s.vpos = reinterpret_cast<int*>(smem_raw + L.vpos);
   s.xr = reinterpret_cast<double*>(smem_raw + L.ext);
   s.yr = s.xr + round_up(ca.max_m + 1, 4);
   s.redP = reinterpret_cast<Key*>(smem_raw + L.red);

@@ -96,7 +96,11 @@ class Plan:
             K, nt, sm, cnt = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
             N.check(self._L.blpg_plan_class_info(self._h, i, C.byref(K), C.byref(nt),
                                                  C.byref(sm), C.byref(cnt)), "class_info")
-            out.append(dict(cluster=K.value, threads=nt.value, smem=sm.value, lps=cnt.value))
+            per_sm, grid = C.c_int32(), C.c_int32()
+            N.check(self._L.blpg_plan_class_residency(self._h, i, C.byref(per_sm), C.byref(grid)),
+                    "class_residency")
+            out.append(dict(cluster=K.value, threads=nt.value, smem=sm.value, lps=cnt.value,
+                            ctas_per_sm=per_sm.value, grid=grid.value))
         return out
 
     def launches(self) -> int:
