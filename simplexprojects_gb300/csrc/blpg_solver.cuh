@@ -158,7 +158,8 @@ struct Layout {
     vpos = off;  // slot of every nonbasic variable, -1 - row of a basic one
     off += nvp * 4;
     ext = off;
-    if (elem == 4) off += 2 * mp1 * 8;  // FP64 x_B and duals of the refresh
+    // FP32 tableau: FP64 x_B and duals of the refresh, FP32 residual copy
+    if (elem == 4) off += 2 * mp1 * 8 + mp1 * 4;
     red = off;
     off += 3 * 32 * 16;  // three argmin scratch buffers (pricing, ratio, Harris)
     state = off;
@@ -334,6 +335,7 @@ struct Solver {
   int* vpos;   // variable -> slot if nonbasic, -1 - row if basic
   double* xr;  // FP32 tableau only: FP64 x_B of the refresh
   double* yr;  // FP32 tableau only: FP64 duals of the refresh
+  float* rf;   // FP32 tableau only: the refresh's residuals rounded to FP32
   Key* redP;
   Key* redR;
   Key* redH;
@@ -535,35 +537,42 @@ struct Solver {
     const int sl = local_slot(s, c0, cw);
     const bool has_s = sl >= lane * V && sl < lane * V + V;
     const int se = sl - lane * V;
-    // kU rows per step, every load issued before any store (rows
-    // grp, grp + G, ... are disjoint, so this only adds memory parallelism)
-    constexpr int kU = 1;  // measured: deeper unrolling of the sweep is slower
-    for (int i0 = grp; i0 < m; i0 += kU * G) {
+    // kU rows per step, every load issued before any store (rows grp,
+    // grp + G, ... are disjoint, so this only adds parallelism).  Row r
+    // already holds the divided pivot row and is only read.
+    constexpr int kU = 2;
+    int i0 = grp;
+    for (; i0 + (kU - 1) * G < m; i0 += kU * G) {
       T f[kU];
       VT t[kU];
 #pragma unroll
       for (int u = 0; u < kU; ++u) {
         const int i = i0 + u * G;
-        if (i < m) {
-          f[u] = pcol[i];
-          t[u] = *reinterpret_cast<const VT*>(tb + (size_t)i * ldw + lane * V);
-        }
+        f[u] = pcol[i];
+        t[u] = *reinterpret_cast<const VT*>(tb + (size_t)i * ldw + lane * V);
       }
 #pragma unroll
       for (int u = 0; u < kU; ++u) {
         const int i = i0 + u * G;
-        if (i < m) {
-          if (i == r) {
-            t[u] = p;
-          } else if (f[u] != T(0)) {  // a zero multiplier leaves the row as it is
-            if (has_s) vset(t[u], se, T(0));
-            t[u] = v_fma(f[u], p, t[u]);
-            *reinterpret_cast<VT*>(tb + (size_t)i * ldw + lane * V) = t[u];
-          }
-          if (has_q) colx_next[i] = vget<VT, T>(t[u], qe);
-          if (has_rhs) rhsx[i] = vget<VT, T>(t[u], 0);
+        if (f[u] != T(0) && i != r) {  // a zero multiplier leaves the row as it is
+          if (has_s) vset(t[u], se, T(0));
+          t[u] = v_fma(f[u], p, t[u]);
+          *reinterpret_cast<VT*>(tb + (size_t)i * ldw + lane * V) = t[u];
         }
+        if (has_q) colx_next[i] = vget<VT, T>(t[u], qe);
+        if (has_rhs) rhsx[i] = vget<VT, T>(t[u], 0);
       }
+    }
+    for (; i0 < m; i0 += G) {
+      const T f = pcol[i0];
+      VT t = *reinterpret_cast<const VT*>(tb + (size_t)i0 * ldw + lane * V);
+      if (f != T(0) && i0 != r) {
+        if (has_s) vset(t, se, T(0));
+        t = v_fma(f, p, t);
+        *reinterpret_cast<VT*>(tb + (size_t)i0 * ldw + lane * V) = t;
+      }
+      if (has_q) colx_next[i0] = vget<VT, T>(t, qe);
+      if (has_rhs) rhsx[i0] = vget<VT, T>(t, 0);
     }
     if (has_q && grp == 0) colx_next[m] = tb[(size_t)m * ldw + qloc];
   }
@@ -889,13 +898,18 @@ struct Solver {
   }
 
   // FP64 refresh of the FP32 tableau: x_B and the duals y are recomputed
-  // from the original A, b, c with one step of iterative refinement each
-  // (residual in FP64, correction through B^-1 = the slack columns of the
-  // tableau in FP32), then d_j = y^T a_j - c_j and z = c_B^T x_B in FP64.
-  // The FP32 RHS column (every replica) and objective row are overwritten.
-  // Rank 0 computes, reading and writing the other CTAs' columns through
-  // distributed shared memory.  Returns bit 0: x_B >= -ptol, bit 1:
-  // d >= -opt_tol (both judged in FP64).  Single-phase LPs only.
+  // from the original A, b, c with iterative refinement (residual in FP64,
+  // correction through B^-1 in FP32; the columns of B^-1 are the slack
+  // columns: stored ones for nonbasic slacks, unit vectors for basic ones),
+  // then d_j = y^T a_j - c_j for the nonbasic columns and z = c_B^T x_B in
+  // FP64.  The FP32 RHS column (every replica) and objective row are
+  // overwritten.  Rank 0 computes, reading and writing the other CTAs'
+  // columns through distributed shared memory.  Every sum runs in a fixed
+  // order, so the result does not depend on the thread count or the cluster
+  // split.  All work is proportional to ns, the number of structural basics
+  // (= the number of nonbasic slacks), except the reduced costs, one FP64
+  // dot product per nonbasic structural column.  Returns bit 0: x_B >= -ptol,
+  // bit 1: d >= -opt_tol (both judged in FP64).  Single-phase LPs only.
   __device__ int refresh(const Geom& g, const double* A, const double* b, const double* c,
                          const LpArgs& a) {
     const int m = g.m, n = g.n;
@@ -904,39 +918,50 @@ struct Solver {
     if (CLUSTER) csync();
     int ok = 0;
     if (rank == 0) {
-      double* res = reinterpret_cast<double*>(col0);  // col0|col1: m doubles
-      // Structural basics as a compact list of rows, in row order; flags[]
-      // holds it (its warm-start use is over by now).  The row where slack k
-      // is basic is -1 - vpos[n + k] (vpos[n + k] < 0).
+      double* res = reinterpret_cast<double*>(col0);   // col0|col1: m doubles
+      double* part = reinterpret_cast<double*>(redP);  // 192 doubles of partial sums
+      // Structural basics as a list of rows in row order (flags[], its
+      // warm-start use is over by now); nonbasic slacks as a list of slack
+      // indices k in increasing order (rhsx, free until the next pivot).
+      // Slack k sits in slot vpos[n + k] when nonbasic; when basic, in row
+      // -1 - vpos[n + k].
       int* slist = flags;
-      int* wcount = reinterpret_cast<int*>(redH);  // per-32-row chunk counts (<= 128)
-      const int nchunks = ceil_div(m, 32);
-      // row-ordered compaction: ballot per 32-row chunk, then a prefix sum
-      for (int ch = warp; ch < nchunks; ch += nw) {
-        const int i = ch * 32 + lane;
-        const bool st = i < m && basis[i] < n;
+      int* nlist = reinterpret_cast<int*>(rhsx);
+      int* wcount = reinterpret_cast<int*>(redH);  // chunk offsets: [0,33) rows, [64,97) slacks
+      const int nch = ceil_div(m, 32);
+      for (int ch = warp; ch < 2 * nch; ch += nw) {
+        const bool rows = ch < nch;
+        const int i = (rows ? ch : ch - nch) * 32 + lane;
+        const bool st = i < m && (rows ? basis[i] < n : vpos[n + i] >= 0);
         const unsigned bal = __ballot_sync(0xffffffffu, st);
-        if (lane == 0) wcount[ch] = __popc(bal);
+        if (lane == 0) wcount[rows ? ch : 64 + ch - nch] = __popc(bal);
       }
       __syncthreads();
-      if (tid == 0) {
+      if (tid < 2) {
         int acc = 0;
-        for (int ch = 0; ch < nchunks; ++ch) {
-          const int v = wcount[ch];
-          wcount[ch] = acc;
+        for (int ch = 0; ch < nch; ++ch) {
+          const int v = wcount[64 * tid + ch];
+          wcount[64 * tid + ch] = acc;
           acc += v;
         }
-        wcount[nchunks] = acc;
+        wcount[64 * tid + nch] = acc;
       }
       __syncthreads();
-      for (int ch = warp; ch < nchunks; ch += nw) {
-        const int i = ch * 32 + lane;
-        const bool st = i < m && basis[i] < n;
+      for (int ch = warp; ch < 2 * nch; ch += nw) {
+        const bool rows = ch < nch;
+        const int i = (rows ? ch : ch - nch) * 32 + lane;
+        const bool st = i < m && (rows ? basis[i] < n : vpos[n + i] >= 0);
         const unsigned bal = __ballot_sync(0xffffffffu, st);
-        if (st) slist[wcount[ch] + __popc(bal & ((1u << lane) - 1u))] = i;
+        const int pos = __popc(bal & ((1u << lane) - 1u));
+        if (st) {
+          if (rows)
+            slist[wcount[ch] + pos] = i;
+          else
+            nlist[wcount[64 + ch - nch] + pos] = i;
+        }
       }
       __syncthreads();
-      const int ns = wcount[nchunks];
+      const int ns = wcount[nch], nn = wcount[64 + nch];
       // Largest |correction| and |value| of a refinement step: positive
       // floats order like their bit patterns, so a shared atomicMax works.
       unsigned* mx = &sh->aux.w2;  // [0] max |correction|, [1] max |value|
@@ -944,43 +969,58 @@ struct Solver {
       for (int it = 0; it < 2; ++it) {
         if (tid == 0) mx[0] = mx[1] = 0u;
         __syncthreads();
-        // res_k = b_k - sum over structural basics A_k,bi x_i - x_(slack k)
-        // four threads per row k (a quad of lanes), each summing every 4th
-        // structural basic; the quad combines in a fixed order
-        // warp-uniform trip count: every lane reaches the shuffles
-        for (int wb = tid & ~31; wb < 4 * m; wb += nt) {
-          const int k = (wb + lane) >> 2, q = lane & 3;
-          double part = 0.0;
-          if (k < m) {
-            const double* Ak = A + (size_t)k * n;
-#pragma unroll 4
-            for (int t = q; t < ns; t += 4) {
-              const int i = slist[t];
-              part = fma(Ak[basis[i]], xr[i], part);
-            }
+        // r_k = b_k - sum_t A_k,col_t x_t - x_(slack k, when basic): one
+        // thread per row, four interleaved partial sums over the basics
+        for (int k = tid; k < m; k += nt) {
+          const double* Ak = A + (size_t)k * n;
+          double p0 = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;
+          int t = 0;
+          for (; t + 4 <= ns; t += 4) {
+            const int i0 = slist[t], i1 = slist[t + 1], i2 = slist[t + 2], i3 = slist[t + 3];
+            p0 = fma(__ldg(Ak + basis[i0]), xr[i0], p0);
+            p1 = fma(__ldg(Ak + basis[i1]), xr[i1], p1);
+            p2 = fma(__ldg(Ak + basis[i2]), xr[i2], p2);
+            p3 = fma(__ldg(Ak + basis[i3]), xr[i3], p3);
           }
-          const double p1 = __shfl_xor_sync(0xffffffffu, part, 1);
-          const double s01 = (q & 1) ? p1 + part : part + p1;
-          const double p2 = __shfl_xor_sync(0xffffffffu, s01, 2);
-          const double sum = (q & 2) ? p2 + s01 : s01 + p2;
-          if (k < m && q == 0) {
-            double r = b[k] - sum;
-            const int sv = vpos[n + k];
-            if (sv < 0) r = r - xr[-1 - sv];
-            res[k] = r;
+          for (; t < ns; ++t) {
+            const int i0 = slist[t];
+            p0 = fma(__ldg(Ak + basis[i0]), xr[i0], p0);
           }
+          double r = b[k] - ((p0 + p1) + (p2 + p3));
+          const int sv = vpos[n + k];
+          if (sv < 0) r = r - xr[-1 - sv];
+          res[k] = r;
+          rf[k] = (float)r;
         }
         __syncthreads();
-        for (int i = warp; i < m; i += nw) {
+        // dx_i = sum_k Binv_ik r_k in FP32: one thread per row i over the
+        // nonbasic slacks' columns, plus r_k when row i holds basic slack k
+        for (int ib = tid & ~31; ib < m; ib += nt) {  // warp-uniform trip count
+          const int i = ib + lane;
           float acc = 0.f;
-          for (int k = lane; k < m; k += 32)
-            acc = fmaf((float)binv(g, i, k), (float)res[k], acc);
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-          if (lane == 0) {
+          if (i < m) {
+            float q0 = 0.f, q1 = 0.f;
+            int u = 0;
+            for (; u + 2 <= nn; u += 2) {
+              const int k0 = nlist[u], k1 = nlist[u + 1];
+              q0 = fmaf((float)*elem(g, i, vpos[n + k0]), rf[k0], q0);
+              q1 = fmaf((float)*elem(g, i, vpos[n + k1]), rf[k1], q1);
+            }
+            if (u < nn) {
+              const int k0 = nlist[u];
+              q0 = fmaf((float)*elem(g, i, vpos[n + k0]), rf[k0], q0);
+            }
+            acc = q0 + q1;
+            const int bi = basis[i];
+            if (bi >= n && bi < n + m) acc = acc + rf[bi - n];
             xr[i] += (double)acc;
-            atomicMax(&mx[0], __float_as_uint(fabsf(acc)));
-            atomicMax(&mx[1], __float_as_uint(fabsf((float)xr[i])));
+          }
+          const unsigned c0m = __reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(acc)));
+          const unsigned c1m =
+              __reduce_max_sync(0xffffffffu, i < m ? __float_as_uint(fabsf((float)xr[i])) : 0u);
+          if (lane == 0) {
+            atomicMax(&mx[0], c0m);
+            atomicMax(&mx[1], c1m);
           }
         }
         __syncthreads();
@@ -993,91 +1033,111 @@ struct Solver {
         const int sv = vpos[n + k];
         yr[k] = sv >= 0 ? (double)*elem(g, m, sv) : 0.0;
       }
+      // the k range of each structural basic's column sum is split in P
+      // parts (partial sums in `part`, 192 doubles), combined in a fixed
+      // order; P = 1 above 96 basics
+      const int P = (ns > 0 && ns <= 96) ? min(4, 192 / ns) : 1;
+      const int kc = ceil_div(m, P);
       for (int it = 0; it < 2; ++it) {
         if (tid == 0) mx[0] = mx[1] = 0u;
         __syncthreads();
-        // s_i = cB_i - (B^T y)_i: slack basics -y_(bi-n); structural basics
-        // c_bi - A_(:,bi)^T y, one warp per column (lanes over rows)
+        // s_i = cB_i - (B^T y)_i: structural basic in row i with column col:
+        // c_col - sum_k A_k,col y_k; basic slack k: -y_k
+        for (int w = tid; w < ns * P; w += nt) {
+          const int t = w % ns, pp = w / ns;
+          const int col = basis[slist[t]];
+          const int k0 = pp * kc, k1 = min(m, k0 + kc);
+          double p0 = 0.0, p1 = 0.0;
+          int k = k0;
+          for (; k + 2 <= k1; k += 2) {
+            p0 = fma(__ldg(A + (size_t)k * n + col), yr[k], p0);
+            p1 = fma(__ldg(A + (size_t)(k + 1) * n + col), yr[k + 1], p1);
+          }
+          if (k < k1) p0 = fma(__ldg(A + (size_t)k * n + col), yr[k], p0);
+          if (P == 1) {
+            const double sv = c[col] - (p0 + p1);
+            res[slist[t]] = sv;
+            rf[slist[t]] = (float)sv;
+          } else
+            part[pp * ns + t] = p0 + p1;
+        }
         for (int i = tid; i < m; i += nt) {
           const int bi = basis[i];
-          if (bi >= n) res[i] = bi < n + m ? -yr[bi - n] : 0.0;
-        }
-        for (int t = warp; t < ns; t += nw) {
-          const int i = slist[t], bi = basis[i];
-          double acc = 0.0;
-#pragma unroll 4
-          for (int k = lane; k < m; k += 32) acc = fma(A[(size_t)k * n + bi], yr[k], acc);
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-          if (lane == 0) res[i] = c[bi] - acc;
+          if (bi >= n) {
+            const double sv = bi < n + m ? -yr[bi - n] : 0.0;
+            res[i] = sv;
+            rf[i] = (float)sv;
+          }
         }
         __syncthreads();
-        // dy_k = sum_i s_i Binv_ik.  With m <= 192 two halves of the rows per
-        // column are summed by separate threads into the (idle) argmin
-        // scratch and combined in a fixed order; larger m in one pass.
-        float* half = reinterpret_cast<float*>(redP);  // 1536 B: 2 x m floats for m <= 192
-        const int H = 2 * m <= 3 * 32 * 4 ? 2 : 1;
-        const int mh = (m + H - 1) / H;
-        for (int w = tid; w < H * m; w += nt) {
-          const int k = w % m, h = w / m;
-          const int i0 = h * mh, i1 = min(m, i0 + mh);
-          const int sv = vpos[n + k];
+        for (int t = tid; t < ns && P > 1; t += nt) {
+          double sum = part[t];
+          for (int pp = 1; pp < P; ++pp) sum += part[pp * ns + t];
+          const int i = slist[t];
+          res[i] = c[basis[i]] - sum;
+          rf[i] = (float)res[i];
+        }
+        __syncthreads();
+        // dy_k = sum_i s_i Binv_ik in FP32: a basic slack k in row i takes
+        // s_i, a nonbasic one sums its stored column (one thread per slack)
+        for (int kb = tid & ~31; kb < m; kb += nt) {  // warp-uniform trip count
+          const int k = kb + lane;
           float acc = 0.f;
-          if (sv >= 0) {
-#pragma unroll 4
-            for (int i = i0; i < i1; ++i) acc = fmaf((float)res[i], (float)*elem(g, i, sv), acc);
-          } else {
-            // basic slack: column k of B^-1 is the unit vector of its row
-            const int row = -1 - sv;
-            if (row >= i0 && row < i1) acc = (float)res[row];
-          }
-          if (H == 2) {
-            half[h * m + k] = acc;
-          } else {
+          if (k < m) {
+            const int sv = vpos[n + k];
+            if (sv < 0) {
+              acc = rf[-1 - sv];
+            } else {
+              float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f;
+              int i = 0;
+              for (; i + 4 <= m; i += 4) {
+                q0 = fmaf(rf[i], (float)*elem(g, i, sv), q0);
+                q1 = fmaf(rf[i + 1], (float)*elem(g, i + 1, sv), q1);
+                q2 = fmaf(rf[i + 2], (float)*elem(g, i + 2, sv), q2);
+                q3 = fmaf(rf[i + 3], (float)*elem(g, i + 3, sv), q3);
+              }
+              for (; i < m; ++i) q0 = fmaf(rf[i], (float)*elem(g, i, sv), q0);
+              acc = (q0 + q1) + (q2 + q3);
+            }
             yr[k] += (double)acc;
-            atomicMax(&mx[0], __float_as_uint(fabsf(acc)));
-            atomicMax(&mx[1], __float_as_uint(fabsf((float)yr[k])));
+          }
+          const unsigned c0m = __reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(acc)));
+          const unsigned c1m =
+              __reduce_max_sync(0xffffffffu, k < m ? __float_as_uint(fabsf((float)yr[k])) : 0u);
+          if (lane == 0) {
+            atomicMax(&mx[0], c0m);
+            atomicMax(&mx[1], c1m);
           }
         }
         __syncthreads();
-        if (H == 2) {
-          for (int k = tid; k < m; k += nt) {
-            const float acc = half[k] + half[m + k];
-            yr[k] += (double)acc;
-            atomicMax(&mx[0], __float_as_uint(fabsf(acc)));
-            atomicMax(&mx[1], __float_as_uint(fabsf((float)yr[k])));
-          }
-          __syncthreads();
-        }
         if (__uint_as_float(mx[0]) <= 1e-10f * fmaxf(1.f, __uint_as_float(mx[1]))) break;
         __syncthreads();
       }
-      // Reduced costs d_j = y^T a_j - c_j for structural j: a quad of lanes
-      // per column, lane q summing rows q, q + 4, ...; the quad combines in a
-      // fixed order and its first lane writes d_j.  Slack k: d = y_k.
+      // Reduced costs d_j = y^T a_j - c_j of the nonbasic structural
+      // columns: one thread per column over coalesced rows of A, four
+      // interleaved partial sums.  Nonbasic slack k: d = y_k.
       bool badd = false, badp = false;
-      for (int wb = tid & ~31; wb < 4 * n; wb += nt) {  // warp-uniform trip count
-        const int j = (wb + lane) >> 2, q = lane & 3;
-        double part = 0.0;
-        if (j < n) {
-#pragma unroll 8
-          for (int k = q; k < m; k += 4) part = fma(A[(size_t)k * n + j], yr[k], part);
+      for (int j = tid; j < n; j += nt) {
+        const int sv = vpos[j];
+        if (sv < 0) continue;
+        double p0 = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;
+        int k = 0;
+        for (; k + 4 <= m; k += 4) {
+          p0 = fma(__ldg(A + (size_t)k * n + j), yr[k], p0);
+          p1 = fma(__ldg(A + (size_t)(k + 1) * n + j), yr[k + 1], p1);
+          p2 = fma(__ldg(A + (size_t)(k + 2) * n + j), yr[k + 2], p2);
+          p3 = fma(__ldg(A + (size_t)(k + 3) * n + j), yr[k + 3], p3);
         }
-        const double p1 = __shfl_xor_sync(0xffffffffu, part, 1);
-        const double s01 = (q & 1) ? p1 + part : part + p1;
-        const double p2 = __shfl_xor_sync(0xffffffffu, s01, 2);
-        const double sum = (q & 2) ? p2 + s01 : s01 + p2;
-        if (j < n && q == 0) {
-          const double d = sum - c[j];
-          const int sv = vpos[j];
-          if (sv >= 0) *elem(g, m, sv) = (T)d;
-          badd = badd || d < -a.opt_tol;
-        }
+        for (; k < m; ++k) p0 = fma(__ldg(A + (size_t)k * n + j), yr[k], p0);
+        const double d = ((p0 + p1) + (p2 + p3)) - c[j];
+        *elem(g, m, sv) = (T)d;
+        badd = badd || d < -a.opt_tol;
       }
       for (int k = tid; k < m; k += nt) {
-        const double d = yr[k];
         const int sv = vpos[n + k];
-        if (sv >= 0) *elem(g, m, sv) = (T)d;
+        if (sv < 0) continue;
+        const double d = yr[k];
+        *elem(g, m, sv) = (T)d;
         badd = badd || d < -a.opt_tol;
       }
       for (int i = tid; i < m; i += nt) {
@@ -1090,9 +1150,9 @@ struct Solver {
       }
       if (tid == 0) {
         double z = 0.0;
-        for (int i = 0; i < m; ++i) {
-          const int bi = basis[i];
-          if (bi < n) z = fma(c[bi], xr[i], z);
+        for (int t = 0; t < ns; ++t) {
+          const int i = slist[t];
+          z = fma(c[basis[i]], xr[i], z);
         }
         sh->z = z;
         for (int o = 0; o < K; ++o) {
@@ -1170,28 +1230,60 @@ struct Solver {
       }
     }
     __syncthreads();
-    for (int i = warp; i <= m; i += nw) {
-      const bool neg = i < m && na > 0 && flags[i] >= 0;
-      T* row = tab + (size_t)i * g.ldw;
-      for (int lj = lane; lj < g.ldw; lj += 32) {
-        T v = T(0);
-        if (lj < lc) {
-          const int s = c0 + lj;
-          if (s < n) {
-            if (i < m) {
-              const T av = (T)A[(size_t)i * n + s];
-              v = neg ? -av : av;
-            } else if (na == 0) {
-              v = -(T)c[s];
+    // Tableau entries in row-major order, eight per thread per round: the
+    // round's source addresses are chosen first and its eight loads issued
+    // unconditionally (entries with no source read b[0]), so they are all in
+    // flight before the first conversion waits on one.
+    const int ldw = g.ldw;
+    const int di = nt / ldw, dl = nt - di * ldw;
+    int i = tid / ldw, lj = tid - i * ldw;
+    while (i <= m) {
+      const double* src[8];
+      int at[8], kind[8];  // kind: 0 zero, 1 value, 2 negated value, 3 -1
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        at[u] = -1;
+        kind[u] = 0;
+        src[u] = b;
+        if (i <= m) {
+          at[u] = i * ldw + lj;
+          const bool neg = i < m && na > 0 && flags[i] >= 0;
+          if (lj < lc) {
+            const int s = c0 + lj;
+            if (s < n) {
+              if (i < m) {
+                src[u] = A + (size_t)i * n + s;
+                kind[u] = neg ? 2 : 1;
+              } else if (na == 0) {
+                src[u] = c + s;
+                kind[u] = 2;
+              }
+            } else if (i < m && cvar[s] - n == i) {
+              kind[u] = 3;  // the negated row's slack
             }
-          } else if (i < m && cvar[s] - n == i) {
-            v = T(-1);  // the negated row's slack
+          } else if (lj == g.cw && i < m) {
+            src[u] = b + i;
+            kind[u] = neg ? 2 : 1;
           }
-        } else if (lj == g.cw && i < m) {
-          const T bv = (T)b[i];
-          v = neg ? -bv : bv;
+          lj += dl;
+          i += di;
+          if (lj >= ldw) {
+            lj -= ldw;
+            ++i;
+          }
         }
-        row[lj] = v;
+      }
+      double raw[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) raw[u] = __ldg(src[u]);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (at[u] < 0) continue;
+        T v = T(0);
+        if (kind[u] == 1) v = (T)raw[u];
+        else if (kind[u] == 2) v = -(T)raw[u];
+        else if (kind[u] == 3) v = T(-1);
+        tab[at[u]] = v;
       }
     }
     __syncthreads();
@@ -1263,14 +1355,9 @@ struct Solver {
         if (a.hint) {
           info |= kInfoWarm;
           if (crash(g, c0, a.hint + a.offbasis[lp], a, pivots, cur, lc) > 0) info |= kInfoPartial;
-          int fl;
-          if (kFP32) {
-            fl = refresh(g, A, b, c, a);
-            refreshed = true;
-            info |= kInfoRefresh;
-          } else {
-            fl = check_feasible(g, c0, lc, ptol, opt_tol);
-          }
+          // feasibility of the crashed basis judged on the tableau itself
+          // (the final FP64 refresh verifies whatever basis the finish ends on)
+          const int fl = check_feasible(g, c0, lc, ptol, opt_tol);
           if (fl & 1) {
             st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
           } else if (fl & 2) {
@@ -1394,6 +1481,7 @@ __global__ void __launch_bounds__(512, 1) solve_kernel(const LpArgs a, const Cla
   s.vpos = reinterpret_cast<int*>(smem_raw + L.vpos);
   s.xr = reinterpret_cast<double*>(smem_raw + L.ext);
   s.yr = s.xr + round_up(ca.max_m + 1, 4);
+  s.rf = reinterpret_cast<float*>(s.yr + round_up(ca.max_m + 1, 4));
   s.redP = reinterpret_cast<Key*>(smem_raw + L.red);
   s.redR = s.redP + 32;
   s.redH = s.redP + 64;
