@@ -3,7 +3,10 @@
 Default workload: kind 3 (the metric's configuration): 64 base LPs (m=174,
 n=142), 40,000 perturbed instances solved by the plain FP64 solver to train
 the warm-start network, 10,000 held-out instances timed with the learned warm
-start + FP32 tableau (value) beside the plain FP64 cold solver (plain_fp64).
+start + FP32 tableau (value: the network's basis probabilities weight
+steepest-edge pricing) beside the plain FP64 cold solver (plain_fp64, the
+reference's Dantzig method) and, in `variants`, the crash-mode warm start and
+the cold FP32 solver under both pricing rules.
 
 Workloads are the synthetic configurations of include/blpg.h (seeded,
 deterministic; they stand in for the Netlib-sized LPs the reference was run
@@ -14,12 +17,13 @@ on).  One step = one solve of the whole workload batch.
   e2e          LPs/s through the public C ABI (blpg_solve_batch) from host
                buffers: host->device copy of A, b, c and device->host copy of
                status/objective/pivots inside the timed region
-  roofline     algorithmic bytes per pivot  s * (2 (m+1) W + W + 2 (m+1)),
-               W = n + m + 1, s = 8 (FP64) / 4 (FP32), summed over the LPs'
-               pivots, divided by the CUDA-event time of the solve kernels;
-               peak = shared-memory bandwidth measured live on the device.
-               The FP64 tableau is also bound by the FP64 FMA pipe (one FMA
-               per element per pivot): reported beside it.
+  roofline     algorithmic bytes per pivot of the condensed tableau
+               s * (2 (m+1) W + 4 (m+1)), W = n + 1 stored columns (nonbasic
+               + RHS), s = 8 (FP64) / 4 (FP32), summed over the LPs' pivots,
+               divided by the CUDA-event time of the solve kernels; peak =
+               shared-memory bandwidth measured live on the device.  The FP64
+               tableau is also bound by the FP64 FMA pipe (one FMA per stored
+               element per pivot): reported beside it.
   cpu_baseline the CPU oracle (plain-C restatement of the reference method,
                all host threads) on a bounded sample of the same workload
 
@@ -65,8 +69,12 @@ def workload(kind: int, rank: int = 0, world: int = 1):
 
 
 def bytes_per_pivot(m, n, s):
-    W = n + m + 1
-    return s * (2.0 * (m + 1) * W + W + 2.0 * (m + 1))
+    """Shared-memory bytes one pivot of the condensed tableau must move: the
+    (m + 1) x (n + 1) stored entries (n nonbasic columns + RHS) read and
+    written once, plus the pivot column and RHS extracted (written, then
+    read by the ratio test).  Element size s."""
+    W = n + 1
+    return s * (2.0 * (m + 1) * W + 4.0 * (m + 1))
 
 
 class Clocks:
@@ -188,8 +196,11 @@ def run_learned(args, rank, world, local):
     ws = WarmStart(174, 142, 64, seed=7, device=dev, max_batch=(max(n_eval, 1) + 63) // 64 * 64)
     rep = ws.train(train, tb.basis, epochs=args.epochs, lr=1e-3, batch_size=512)
     del train
-    ls = LearnedSolver(ws, evalb, "fp32")
+    ls = LearnedSolver(ws, evalb, "fp32", mode="guided")
+    crash = LearnedSolver(ws, evalb, "fp32", mode="crash")
     plain = sp.DeviceBatch(evalb, "fp64", device=dev)
+    cold32 = sp.DeviceBatch(evalb, "fp32", device=dev)
+    cold32se = sp.DeviceBatch(evalb, "fp32", device=dev, pricing="steepest")
     setup_s = time.perf_counter() - t_setup
     stream = torch.cuda.current_stream()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
@@ -216,11 +227,23 @@ def run_learned(args, rank, world, local):
         torch.cuda.nvtx.range_pop()
     t_plain = timed(plain.run, args.steps)
     ls.predict()
-    t_solve = timed(lambda: ls.db.run(hint=ls.hint), args.steps)  # the FP32 solve kernels alone
+    t_solve = timed(lambda: ls.db.run(weight=ls.weight), args.steps)  # the FP32 solve alone
     t_pred = timed(ls.predict, args.steps)
     res = ls.result()
     pres = plain.result()
-    hint = ls.hint.cpu().numpy()
+    variants = {}
+    for name, fn, obj in (("learned_crash_fp32_dantzig", crash.run, crash.db),
+                          ("cold_fp32_dantzig", cold32.run, cold32),
+                          ("cold_fp32_steepest", cold32se.run, cold32se)):
+        for _ in range(2):
+            fn()
+        tv = statistics.median(timed(fn, max(3, args.steps // 2)))
+        rv = obj.result()
+        variants[name] = {"value": len(rv.status) * world / (tv * 1e-3), "unit": "LPs/s",
+                          "ms_per_step": tv, "mean_pivots": float(rv.pivots.mean()),
+                          "status_match": float((rv.status == pres.status).mean())}
+    cres = crash.db.result()
+    hint = crash.hint.cpu().numpy()
     plain_b = sp.solve(evalb, "fp64", want_basis=True)
     acc, exact = basis_accuracy(hint, plain_b.basis, 174)
     ms = statistics.median(t_learned)
@@ -246,7 +269,7 @@ def run_learned(args, rank, world, local):
     m, n = 174.0, 142.0
     alg_bytes = float((piv * bytes_per_pivot(m, n, 4)).sum())
     ach = alg_bytes / (ms_solve * 1e-3) / 1e9
-    flops = float((piv * 2.0 * (m + 1) * (n + m + 1)).sum())
+    flops = float((piv * 2.0 * (m + 1) * (n + 1)).sum())
     ach_tf = flops / (ms_solve * 1e-3) / 1e12
     cpu = None if args.no_cpu_baseline else cpu_baseline(evalb, "fp64")
     h2d = int(evalb.A.nbytes + evalb.b.nbytes + evalb.c.nbytes)
@@ -257,7 +280,8 @@ def run_learned(args, rank, world, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator, include/blpg.h)",
         "config": {"workload": WORKLOAD_NAMES[3], "lps": total, "precision": "fp32+fp64 refresh",
-                   "method": "learned warm start (MLP 3x512 bf16) + FP32 tableau",
+                   "method": "learned warm start (MLP 3x512 bf16): network probabilities "
+                             "weight steepest-edge pricing of the FP32 tableau",
                    "train_lps": 40_000, "epochs": args.epochs,
                    "parallelism": "replicas" if world > 1 else "1gpu",
                    "l2": "L2 flushed between iterations",
@@ -265,15 +289,19 @@ def run_learned(args, rank, world, local):
         "pivots_per_s": float(piv.sum()) * world / (ms * 1e-3),
         "plain_fp64": {"value": total / (ms_plain * 1e-3), "unit": "LPs/s", "ms_per_step": ms_plain,
                        "pivots_per_s": float(pres.pivots.sum()) * world / (ms_plain * 1e-3),
-                       "mean_pivots": float(pres.pivots.mean())},
+                       "mean_pivots": float(pres.pivots.mean()),
+                       "method": "FP64 tableau, Dantzig pricing, cold slack basis"},
         "speedup_vs_plain_fp64": ms_plain / ms,
+        "variants": variants,
         "learned": {"mean_pivots": float(piv.mean()),
                     "pivots_saved": 1.0 - float(piv.sum()) / float(pres.pivots.sum()),
-                    "fallback_rate": float(((res.info & 2) > 0).mean()),
-                    "shifted_rate": float(((res.info & 64) > 0).mean()),
-                    "dual_rate": float(((res.info & 8) > 0).mean()),
-                    "primal_feasible_hint_rate": float(((res.info & (8 | 2)) == 0).mean()),
-                    "basis_column_accuracy": acc, "exact_basis_rate": exact,
+                    "pivots_saved_vs_cold_steepest":
+                        1.0 - float(piv.mean()) / variants["cold_fp32_steepest"]["mean_pivots"],
+                    "crash_mode": {"mean_pivots": float(cres.pivots.mean()),
+                                   "fallback_rate": float(((cres.info & 2) > 0).mean()),
+                                   "shifted_rate": float(((cres.info & 64) > 0).mean()),
+                                   "dual_rate": float(((cres.info & 8) > 0).mean()),
+                                   "basis_column_accuracy": acc, "exact_basis_rate": exact},
                     "predict_ms": statistics.median(t_pred), "solve_ms": ms_solve,
                     "train_s": rep.seconds, "setup_s": setup_s,
                     "final_train_bce": rep.losses[-1] if rep.losses else None},
@@ -283,13 +311,14 @@ def run_learned(args, rank, world, local):
                 "d2h_bytes_per_step": int(total * 16), "ms_per_step": e2e_ms},
         "roofline": {"bound": "smem", "achieved": ach, "peak": smem.value, "unit": "GB/s",
                      "frac": ach / smem.value, "traffic": None,
-                     "kernel": "solve_kernel<float> (FP32 tableau pivots)",
+                     "kernel": "solve_kernel<float> (FP32 condensed tableau pivots)",
+                     "bytes_per_pivot": bytes_per_pivot(m, n, 4),
                      "peak_source": "measured live (blpg_measure_peaks: shared-memory stream probe)",
                      "fma_pipe": {"achieved": ach_tf, "peak": f32.value, "unit": "TFLOP/s",
                                   "frac": ach_tf / f32.value, "pipe": "fp32"}},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
-        "gpu_launches": args.steps * (ls.db.plan.launches() + ws.hint_launches(n_eval)),
+        "gpu_launches": args.steps * ls.launches(),
         "step_ms_all": t_learned,
     }
     print(json.dumps(out))
@@ -304,6 +333,8 @@ def main():
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--impl", default="blpg", choices=["blpg", "reference"])
+    ap.add_argument("--pricing", default="dantzig", choices=["dantzig", "steepest"],
+                    help="pricing rule of workloads 0-2, 4 (3 runs every variant)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -336,7 +367,7 @@ def main():
 
     batch, total = workload(args.workload, rank, world)
     s = 8 if args.precision == "fp64" else 4
-    db = sp.DeviceBatch(batch, args.precision, device=f"cuda:{local}")
+    db = sp.DeviceBatch(batch, args.precision, device=f"cuda:{local}", pricing=args.pricing)
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
         db.run()
@@ -345,7 +376,7 @@ def main():
     pivots = res.pivots.astype(np.float64)
     alg_bytes = float((pivots * bytes_per_pivot(batch.m.astype(np.float64),
                                                  batch.n.astype(np.float64), s)).sum())
-    flops = float((pivots * 2.0 * (batch.m + 1.0) * (batch.n + batch.m + 1.0)).sum())
+    flops = float((pivots * 2.0 * (batch.m + 1.0) * (batch.n + 1.0)).sum())
 
     # ---- value: device-resident inputs (larger than L2 for kinds 1-4) ----
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -374,7 +405,7 @@ def main():
     for i in range(args.warmup + args.steps):
         barrier()
         t0 = time.perf_counter()
-        r = sp.solve(batch, args.precision)
+        r = sp.solve(batch, args.precision, pricing=args.pricing)
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             e2e_times.append(dt)
@@ -414,10 +445,12 @@ def main():
         "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
         "data": "synthetic (seeded generator, include/blpg.h)",
         "config": {"workload": WORKLOAD_NAMES[args.workload], "lps": total,
-                   "precision": args.precision, "parallelism": "replicas" if world > 1 else "1gpu",
+                   "precision": args.precision, "pricing": args.pricing,
+                   "parallelism": "replicas" if world > 1 else "1gpu",
                    "l2": "inputs larger than L2; L2 flushed between iterations",
                    "classes": db.plan.classes()},
         "pivots_per_s": float(pivots.sum()) * world / (ms * 1e-3),
+        "mean_pivots": float(pivots.mean()),
         "status_counts": np.bincount(res.status, minlength=7).tolist(),
         "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "LPs/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},

@@ -66,6 +66,12 @@ enum {
   BLPG_FP32 = 1  /* FP32 tableau with FP64 refresh of x_B and reduced costs */
 };
 
+/* Pricing rule of the primal simplex (blpg_options.pricing). */
+enum {
+  BLPG_PRICE_DANTZIG = 0, /* most negative reduced cost (the reference's rule) */
+  BLPG_PRICE_STEEPEST = 1 /* largest d_j^2 / ||column j||^2, exact norms */
+};
+
 /* Largest LP handled: rows and total tableau columns (n + m + 1). */
 #define BLPG_MAX_ROWS 1024
 #define BLPG_MAX_COLS 8192
@@ -130,6 +136,18 @@ typedef struct blpg_options {
                               to primal feasibility, true costs restored,
                               primal simplex); 2 a cold solve from the slack
                               basis */
+  int32_t pricing;         /* BLPG_PRICE_DANTZIG (0, default): the reference's
+                              most negative reduced cost; BLPG_PRICE_STEEPEST:
+                              largest d_j^2 / (1 + sum_i T_ij^2), exact column
+                              norms summed every pivot (no reference
+                              counterpart).  Both fall back to Bland's rule
+                              after bland_after degenerate pivots. */
+  const float* price_weight; /* nullable, steepest edge only (host memory for
+                              blpg_solve_batch): per LP n[k] + m[k] factors
+                              multiplying each variable's score (0..n-1
+                              structural, n..n+m-1 slack), packed in LP order;
+                              the learned warm start passes 1 + p_j, p_j the
+                              network's probability that column j is basic */
 } blpg_options;
 
 /* Per-LP outputs (host memory for blpg_solve_batch, device memory for
@@ -183,6 +201,13 @@ int32_t blpg_plan_create(const blpg_batch* host_shapes, const blpg_options* opt,
 int32_t blpg_plan_execute(blpg_plan* plan, const double* dA, const double* db,
                           const double* dc, const int32_t* basis_hint,
                           blpg_result* dev_out, void* stream);
+/* blpg_plan_execute with steepest-edge score weights in device memory
+ * (n[k] + m[k] floats per LP, packed; see blpg_options.price_weight).  The
+ * plan must have been made with pricing = BLPG_PRICE_STEEPEST. */
+int32_t blpg_plan_execute_weighted(blpg_plan* plan, const double* dA, const double* db,
+                                   const double* dc, const int32_t* basis_hint,
+                                   const float* price_weight, blpg_result* dev_out,
+                                   void* stream);
 
 /* Number of size classes and, per class, CTAs per LP (cluster size),
  * threads per CTA, dynamic shared memory per CTA and LPs in the class. */
@@ -282,6 +307,13 @@ int32_t blpg_features(int32_t count, int32_t m, int32_t n, int32_t families,
                       const double* db, const double* dc,
                       const int32_t* d_family, const float* d_mean,
                       const float* d_std, float* dX, int32_t ldx, void* stream);
+/* Steepest-edge weights from scores (blpg_options.price_weight): for LP k,
+ * d_weight[d_offw[k] + j] = 1 + beta * sigmoid(score[k][j]) over its
+ * n[k] + m[k] columns (max_cols the widest, lds >= max_cols). */
+int32_t blpg_price_weights(const float* d_scores, int32_t lds, int32_t count,
+                           const int32_t* d_m, const int32_t* d_n, int32_t max_cols,
+                           const int64_t* d_offw, float beta, float* d_weight,
+                           void* stream);
 /* Basis hint from scores: for LP k, the m[k] highest-scoring of its
  * n[k] + m[k] columns, in decreasing score order, at d_hint + d_offhint[k]. */
 int32_t blpg_topm_hint(const float* d_scores, int32_t lds, int32_t count,

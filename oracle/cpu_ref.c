@@ -72,6 +72,8 @@ typedef struct {
   const double *A, *b, *c;
   const oref_opts* o;
   const int* hint;
+  const float* weight;
+  const int64_t* offw;
   int* info;
   int* status;
   double* obj;
@@ -92,8 +94,10 @@ static void* worker(void* arg) {
     int piv = 0;
     double ob = 0.0;
     int inf = 0;
+    oref_opts o = *J->o;
+    o.weight = J->weight ? J->weight + J->offw[k] : NULL;
     int st = oref_solve_one(J->m[k], J->n[k], J->A + J->offA[k], J->b + J->offb[k],
-                            J->c + J->offc[k], J->o,
+                            J->c + J->offc[k], &o,
                             J->hint ? J->hint + J->offbasis[k] : NULL, &ob,
                             J->x ? J->x + J->offx[k] : NULL,
                             J->basis ? J->basis + J->offbasis[k] : NULL, &piv, &inf);
@@ -109,18 +113,20 @@ int oref_solve_batch(int count, const int* m, const int* n, const int64_t* offA,
                      const int64_t* offb, const int64_t* offc, const double* A,
                      const double* b, const double* c, const oref_opts* o,
                      int threads, const int* hint, int* status, double* obj,
-                     double* x, int* pivots, int* basis, int* info) {
+                     double* x, int* pivots, int* basis, int* info, const float* weight) {
   if (count < 0 || !m || !n || !A || !b || !c || !o || !status || !obj) return -1;
-  int64_t* own = (int64_t*)malloc(sizeof(int64_t) * 5 * (size_t)(count + 1));
+  int64_t* own = (int64_t*)malloc(sizeof(int64_t) * 6 * (size_t)(count + 1));
   if (!own) return -1;
   int64_t *pA = own, *pb = own + (count + 1), *pc = own + 2 * (count + 1);
   int64_t *px = own + 3 * (count + 1), *pbs = own + 4 * (count + 1);
-  pA[0] = pb[0] = pc[0] = px[0] = pbs[0] = 0;
+  int64_t* pw = own + 5 * (count + 1);
+  pA[0] = pb[0] = pc[0] = px[0] = pbs[0] = pw[0] = 0;
   for (int k = 0; k < count; ++k) {
     pA[k + 1] = pA[k] + (int64_t)m[k] * n[k];
     pb[k + 1] = pb[k] + m[k];
     pc[k + 1] = pc[k] + n[k];
     pbs[k + 1] = pbs[k] + m[k];
+    pw[k + 1] = pw[k] + m[k] + n[k];
   }
   batch_job J;
   memset(&J, 0, sizeof(J));
@@ -142,6 +148,8 @@ int oref_solve_batch(int count, const int* m, const int* n, const int64_t* offA,
   J.pivots = pivots;
   J.basis = basis;
   J.hint = hint;
+  J.weight = weight;
+  J.offw = pw;
   J.info = info;
   pthread_mutex_init(&J.lock, NULL);
   if (threads < 1) threads = 1;

@@ -27,6 +27,8 @@ typedef struct {
   int composite;   /* 1: a hinted basis infeasible both ways is finished by a
                       cost-shifted dual phase instead of a cold solve */
   double shift;    /* size of the cost shift (the shifted d_j lie in [shift, 2 shift)) */
+  int pricing;     /* 0: Dantzig (the reference); 1: steepest edge, exact norms */
+  const float* weight; /* steepest edge: score factor per variable (n + m), or null */
 } oref_opts;
 
 void oref_opts_init(oref_opts* o, int precision);
@@ -38,12 +40,13 @@ int oref_solve_one(int m, int n, const double* A, const double* b,
 
 /* Null offsets = packed.  x (nullable) follows off_c; basis and hint
  * (nullable) are packed m per LP; info (nullable) gets the warm-start bits
- * (1 warm, 2 fallback, 4 partial, 8 dual).  threads = POSIX threads. */
+ * (1 warm, 2 fallback, 4 partial, 8 dual); weight (nullable, steepest edge)
+ * is packed n + m per LP.  threads = POSIX threads. */
 int oref_solve_batch(int count, const int* m, const int* n, const int64_t* offA,
                      const int64_t* offb, const int64_t* offc, const double* A,
                      const double* b, const double* c, const oref_opts* o,
                      int threads, const int* hint, int* status, double* obj,
-                     double* x, int* pivots, int* basis, int* info);
+                     double* x, int* pivots, int* basis, int* info, const float* weight);
 
 #ifdef __cplusplus
 }

@@ -61,6 +61,36 @@ static int FN(price)(const FN(tab_t) * t, int ncols, int bland, REAL opt_tol) {
   return q;
 }
 
+/* Steepest-edge pricing (a rule the reference does not have; the published
+ * Goldfarb-Reid criterion with exact norms): among d_j < -opt_tol the
+ * largest d_j^2 / (1 + sum_{i<m} T_ij^2), times weight[j] when given,
+ * lowest index on ties.  The score is rounded to float as on the GPU, whose
+ * norms are fixed-point sums; near-ties may therefore resolve differently
+ * there, so this mode is checked on statuses and objectives, not bit for
+ * bit. */
+static int FN(price_se)(const FN(tab_t) * t, int ncols, REAL opt_tol, const float* weight) {
+  const REAL* d = &TT(t, t->m, 0);
+  int q = -1;
+  float best = 0.f;
+  for (int j = 0; j < ncols; ++j) {
+    const REAL v = d[j];
+    if (!(v < -opt_tol)) continue;
+    double g = 1.0;
+    for (int i = 0; i < t->m; ++i) {
+      const double a = (double)TT(t, i, j);
+      g += a * a;
+    }
+    const float vf = (float)v;
+    float sc = (float)((double)vf * (double)vf / g);
+    if (weight) sc *= weight[j];
+    if (q < 0 || sc > best) {
+      q = j;
+      best = sc;
+    }
+  }
+  return q;
+}
+
 /* Leaving row for entering column q; -1 if no entry exceeds piv_tol.
  * Textbook rule (Bland mode): minimum ratio, ties by lowest basic variable.
  * Harris rule (default): pass 1 bounds the step by the ratios relaxed by
@@ -137,7 +167,8 @@ static int FN(simplex_loop)(FN(tab_t) * t, int ncols, const oref_opts* o,
                             int* pivots, int* bland, int* degen, REAL* f) {
   const REAL opt_tol = (REAL)o->opt_tol, piv_tol = (REAL)o->piv_tol;
   for (;;) {
-    int q = FN(price)(t, ncols, *bland, opt_tol);
+    int q = o->pricing == 1 && !*bland ? FN(price_se)(t, ncols, opt_tol, o->weight)
+                                       : FN(price)(t, ncols, *bland, opt_tol);
     if (q < 0) return OREF_OPT;
     if (*pivots >= o->max_pivots) return OREF_UNDEF;
     REAL theta;

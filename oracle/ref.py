@@ -24,7 +24,7 @@ class Opts(C.Structure):
         ("refactor_period", C.c_int), ("opt_tol", C.c_double), ("piv_tol", C.c_double),
         ("phase1_tol", C.c_double), ("deg_tol", C.c_double), ("feas_tol", C.c_double),
         ("harris", C.c_int), ("ptol", C.c_double), ("composite", C.c_int),
-        ("shift", C.c_double),
+        ("shift", C.c_double), ("pricing", C.c_int), ("weight", C.POINTER(C.c_float)),
     ]
 
 
@@ -41,7 +41,8 @@ def lib():
         L.oref_opts_init.restype = None
         ip, lp, dp = C.POINTER(C.c_int), C.POINTER(C.c_int64), C.POINTER(C.c_double)
         L.oref_solve_batch.argtypes = [C.c_int, ip, ip, lp, lp, lp, dp, dp, dp, C.POINTER(Opts),
-                                       C.c_int, ip, ip, dp, dp, ip, ip, ip]
+                                       C.c_int, ip, ip, dp, dp, ip, ip, ip,
+                                       C.POINTER(C.c_float)]
         L.oref_solve_batch.restype = C.c_int
         L.oref_solve_one.argtypes = [C.c_int, C.c_int, dp, dp, dp, C.POINTER(Opts), ip, dp, dp, ip,
                                      ip, ip]
@@ -50,10 +51,15 @@ def lib():
     return _lib
 
 
+PRICING = {"dantzig": 0, "steepest": 1}
+
+
 def opts(precision: str = "fp64", **kw) -> Opts:
     o = Opts()
     lib().oref_opts_init(C.byref(o), 1 if precision == "fp32" else 0)
     for k, v in kw.items():
+        if k == "pricing" and isinstance(v, str):
+            v = PRICING[v]
         setattr(o, k, v)
     return o
 
@@ -73,8 +79,9 @@ def _p(a, t):
 
 
 def solve_batch(batch, precision: str = "fp64", threads: Optional[int] = None, want_x=False,
-                want_basis=False, hint=None, **kw) -> RefResult:
-    """Solve a simplexprojects_gb300.LPBatch on the CPU with the oracle."""
+                want_basis=False, hint=None, weight=None, **kw) -> RefResult:
+    """Solve a simplexprojects_gb300.LPBatch on the CPU with the oracle.
+    `weight` (steepest-edge pricing only): n[k] + m[k] score factors per LP."""
     L = lib()
     k = batch.count
     m = batch.m.astype(np.int32)
@@ -89,6 +96,9 @@ def solve_batch(batch, precision: str = "fp64", threads: Optional[int] = None, w
     if hint is not None:
         hint = np.ascontiguousarray(hint, dtype=np.int32)
         assert hint.size == int(m.sum())
+    if weight is not None:
+        weight = np.ascontiguousarray(weight, dtype=np.float32)
+        assert weight.size == int((m + n).sum())
     o = opts(precision, **kw)
     if threads is None:
         threads = os.cpu_count() or 1
@@ -96,7 +106,8 @@ def solve_batch(batch, precision: str = "fp64", threads: Optional[int] = None, w
                             _p(ob, C.c_int64), _p(oc, C.c_int64), _p(batch.A, C.c_double),
                             _p(batch.b, C.c_double), _p(batch.c, C.c_double), C.byref(o),
                             int(threads), _p(hint, C.c_int), _p(st, C.c_int), _p(obj, C.c_double),
-                            _p(x, C.c_double), _p(pv, C.c_int), _p(bs, C.c_int), _p(info, C.c_int))
+                            _p(x, C.c_double), _p(pv, C.c_int), _p(bs, C.c_int), _p(info, C.c_int),
+                            _p(weight, C.c_float))
     if rc != 0:
         raise RuntimeError("oref_solve_batch failed")
     return RefResult(st, obj, pv, x, bs, info)

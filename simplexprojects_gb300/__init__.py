@@ -8,12 +8,13 @@ Public API:
     Simplex                         mirror of the reference's host class
 """
 from . import _native
+from ._native import BlpgError
 from .lp import LPBatch, generate, read_abc, WORKLOAD_COUNTS, DEFAULT_SEED
 from .solver import DeviceBatch, Plan, Simplex, SolveResult, options, solve
 
 __all__ = [
     "LPBatch", "generate", "read_abc", "solve", "Plan", "DeviceBatch", "Simplex", "SolveResult",
-    "options", "WORKLOAD_COUNTS", "DEFAULT_SEED",
+    "options", "WORKLOAD_COUNTS", "DEFAULT_SEED", "BlpgError",
 ]
 
 

@@ -39,7 +39,7 @@ class Options(C.Structure):
         ("basis_hint", i32p), ("device", C.c_int32), ("use_graph", C.c_int32),
         ("threads_per_cta", C.c_int32), ("max_cluster", C.c_int32), ("min_cluster", C.c_int32),
         ("cta_smem_budget", C.c_int32), ("ratio_rule", C.c_int32), ("feas_tol", C.c_double),
-        ("warm_mode", C.c_int32),
+        ("warm_mode", C.c_int32), ("pricing", C.c_int32), ("price_weight", C.POINTER(C.c_float)),
     ]
 
 
@@ -57,6 +57,11 @@ SIGNATURES = {
     "blpg_plan_create": (C.c_int32, [C.POINTER(Batch), C.POINTER(Options), C.POINTER(C.c_void_p)]),
     "blpg_plan_execute": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.POINTER(Result), C.c_void_p]),
+    "blpg_price_weights": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                       C.c_int32, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p]),
+    "blpg_plan_execute_weighted": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.c_void_p, C.POINTER(Result),
+                                               C.c_void_p]),
     "blpg_plan_num_classes": (C.c_int32, [C.c_void_p]),
     "blpg_plan_class_info": (C.c_int32, [C.c_void_p, C.c_int32, i32p, i32p, i32p, i32p]),
     "blpg_plan_class_residency": (C.c_int32, [C.c_void_p, C.c_int32, i32p, i32p]),

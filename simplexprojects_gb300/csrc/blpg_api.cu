@@ -92,7 +92,7 @@ struct blpg_plan {
   int precision = BLPG_FP64;
   std::vector<int32_t> m, n, na;
   std::vector<int64_t> offA, offb, offc, offx, offbasis;
-  int64_t extA = 0, extb = 0, extc = 0, extx = 0, extbasis = 0;
+  int64_t extA = 0, extb = 0, extc = 0, extx = 0, extbasis = 0, extw = 0;
   std::vector<blpg::ClassPlan> classes;
   std::vector<int32_t> order;
   // device arrays
@@ -237,6 +237,7 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
     budget = it != g_tuning.threads.end() ? it->second : max_smem;
   }
   budget = std::min(budget, max_smem);
+  const int se = p->opt.pricing == BLPG_PRICE_STEEPEST ? 1 : 0;
   const int min_cluster = std::max(1, std::min(p->opt.min_cluster, max_cluster));
   struct Item {
     int K, nl, ldw, nv;
@@ -251,7 +252,7 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
       for (int K = min_cluster; K <= max_cluster; K *= 2) {
         Geom g(m, n, na, K, V);
         const int nv = n + m + na;
-        if (Layout(m, g.ldw, nv, elem).total <= lim && g.nl <= kMaxThreads) {
+        if (Layout(m, g.ldw, nv, elem, se).total <= lim && g.nl <= kMaxThreads) {
           chosen = K;
           items[k] = {K, g.nl, g.ldw, nv,
                       (double)(m + 1) * (double)(n + na + 1) * (double)(m + n)};
@@ -284,8 +285,9 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
         const int mm = std::max(c.max_m, p->m[lp]);
         const int ll = std::max(c.max_ldw, items[lp].ldw);
         const int vv = std::max(c.max_nv, items[lp].nv);
-        const int lim = std::max(budget, Layout(p->m[lp], items[lp].ldw, items[lp].nv, elem).total);
-        if (Layout(mm, ll, vv, elem).total <= std::min(lim, max_smem)) {
+        const int lim =
+            std::max(budget, Layout(p->m[lp], items[lp].ldw, items[lp].nv, elem, se).total);
+        if (Layout(mm, ll, vv, elem, se).total <= std::min(lim, max_smem)) {
           c.max_m = mm;
           c.max_ldw = ll;
           c.max_nv = vv;
@@ -311,7 +313,7 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
     }
     for (size_t ci = 0; ci < parts.size(); ++ci) {
       ClassPlan c = parts[ci];
-      c.smem = Layout(c.max_m, c.max_ldw, c.max_nv, elem).total;
+      c.smem = Layout(c.max_m, c.max_ldw, c.max_nv, elem, se).total;
       // threads: every member's row of vector lanes at least once (c.nt
       // holds the widest member's lane count here)
       c.nt = pick_threads(p, c.nt, c.smem, kernel_regs<T>(c.K > 1), c.K,
@@ -343,7 +345,7 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
 template <typename T>
 static int launch_one(blpg_plan* p, size_t ci, const LpArgs& args, cudaStream_t s) {
   const ClassPlan& c = p->classes[ci];
-  ClassArgs ca;
+  ClassArgs ca{};
   ca.order = p->d_order + c.order_off;
   ca.count = c.count;
   ca.ticket = p->d_tickets + ci;
@@ -352,6 +354,7 @@ static int launch_one(blpg_plan* p, size_t ci, const LpArgs& args, cudaStream_t 
   ca.max_ldw = c.max_ldw;
   ca.max_na = c.max_na;
   ca.max_nv = c.max_nv;
+  ca.se = p->opt.pricing == BLPG_PRICE_STEEPEST ? 1 : 0;
   if (c.K == 1) {
     dev::solve_kernel<T, false><<<c.grid, c.nt, c.smem, s>>>(args, ca);
     CK(cudaGetLastError());
@@ -555,19 +558,25 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
   CKF(cudaMalloc(&p->d_n, sizeof(int32_t) * Nn));
   CKF(cudaMalloc(&p->d_order, sizeof(int32_t) * Nn));
   CKF(cudaMalloc(&p->d_tickets, sizeof(int32_t) * nc));
-  CKF(cudaMalloc(&p->d_off, sizeof(int64_t) * 5 * Nn));
+  CKF(cudaMalloc(&p->d_off, sizeof(int64_t) * 6 * Nn));
   if (N > 0) {
-    std::vector<int64_t> off(5 * (size_t)N);
+    std::vector<int64_t> off(6 * (size_t)N);
     std::copy(p->offA.begin(), p->offA.end(), off.begin());
     std::copy(p->offb.begin(), p->offb.end(), off.begin() + N);
     std::copy(p->offc.begin(), p->offc.end(), off.begin() + 2 * N);
     std::copy(p->offx.begin(), p->offx.end(), off.begin() + 3 * N);
     std::copy(p->offbasis.begin(), p->offbasis.end(), off.begin() + 4 * N);
+    int64_t acc = 0;  // steepest-edge weights: n + m per LP, packed
+    for (int k = 0; k < N; ++k) {
+      off[5 * (size_t)N + k] = acc;
+      acc += p->n[k] + p->m[k];
+    }
+    p->extw = acc;
     CKF(cudaMemcpy(p->d_m, p->m.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice));
     CKF(cudaMemcpy(p->d_n, p->n.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice));
     CKF(cudaMemcpy(p->d_order, p->order.data(), sizeof(int32_t) * N,
                    cudaMemcpyHostToDevice));
-    CKF(cudaMemcpy(p->d_off, off.data(), sizeof(int64_t) * 5 * N, cudaMemcpyHostToDevice));
+    CKF(cudaMemcpy(p->d_off, off.data(), sizeof(int64_t) * 6 * N, cudaMemcpyHostToDevice));
   }
 #undef CKF
   *out = p.release();
@@ -577,8 +586,17 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
 extern "C" int32_t blpg_plan_execute(blpg_plan* p, const double* dA, const double* db,
                                      const double* dc, const int32_t* basis_hint,
                                      blpg_result* out, void* stream_v) {
+  return blpg_plan_execute_weighted(p, dA, db, dc, basis_hint, nullptr, out, stream_v);
+}
+
+extern "C" int32_t blpg_plan_execute_weighted(blpg_plan* p, const double* dA, const double* db,
+                                              const double* dc, const int32_t* basis_hint,
+                                              const float* price_weight, blpg_result* out,
+                                              void* stream_v) {
   if (!p || !out || !out->status || !out->objective)
     return fail(BLPG_EINVAL, "blpg_plan_execute: null plan or outputs");
+  if (price_weight && p->opt.pricing != BLPG_PRICE_STEEPEST)
+    return fail(BLPG_EINVAL, "blpg_plan_execute: pricing weights need steepest-edge pricing");
   if (p->count == 0) return BLPG_OK;
   if (!dA || !db || !dc) return fail(BLPG_EINVAL, "blpg_plan_execute: null A, b or c");
   CK(cudaSetDevice(p->device));
@@ -592,6 +610,9 @@ extern "C" int32_t blpg_plan_execute(blpg_plan* p, const double* dA, const doubl
   a.offc = p->d_off + 2 * N;
   a.offx = p->d_off + 3 * N;
   a.offbasis = p->d_off + 4 * N;
+  a.offw = p->d_off + 5 * N;
+  a.pricing = p->opt.pricing == BLPG_PRICE_STEEPEST ? 1 : 0;
+  a.weight = price_weight;
   a.A = dA;
   a.b = db;
   a.c = dc;
@@ -712,6 +733,8 @@ static bool plan_matches(const Workspace& w, const blpg_batch* bt, const blpg_op
   blpg_options a = w.key_opt, b = o;
   a.basis_hint = nullptr;
   b.basis_hint = nullptr;
+  a.price_weight = nullptr;
+  b.price_weight = nullptr;
   return w.plan && std::memcmp(&a, &b, sizeof(a)) == 0 && w.key_shapes == shapes &&
          w.key_offs == offs && w.plan->count == bt->count;
 }
@@ -772,9 +795,13 @@ extern "C" int32_t blpg_solve_batch(const blpg_batch* bt, const blpg_options* op
                sob = al(sizeof(double) * N), sx = al(sizeof(double) * p->extx),
                spv = al(sizeof(int32_t) * N), sbs = al(sizeof(int32_t) * p->extbasis);
   const bool hint = opt.basis_hint != nullptr;
+  const bool wt = opt.price_weight != nullptr;
+  if (wt && opt.pricing != BLPG_PRICE_STEEPEST)
+    return fail(BLPG_EINVAL, "blpg_solve_batch: pricing weights need steepest-edge pricing");
+  const size_t sw = al(sizeof(float) * p->extw);
   const size_t need = sA + sb + sc + sst + sob + (out->x ? sx : 0) +
                       (out->pivots ? spv : 0) + (out->basis ? sbs : 0) +
-                      (out->info ? spv : 0) + (hint ? sbs : 0);
+                      (out->info ? spv : 0) + (hint ? sbs : 0) + (wt ? sw : 0);
   if (g_ws.cap < need || g_ws.device != p->device) {
     if (g_ws.buf) cudaFree(g_ws.buf);
     g_ws.buf = nullptr;
@@ -814,14 +841,22 @@ extern "C" int32_t blpg_solve_batch(const blpg_batch* bt, const blpg_options* op
     dhint = (int32_t*)o;
     o += sbs;
   }
+  float* dw = nullptr;
+  if (wt) {
+    dw = (float*)o;
+    o += sw;
+  }
   cudaStream_t s = p->stream;
   if (hint)
     CK(cudaMemcpyAsync(dhint, opt.basis_hint, sizeof(int32_t) * p->extbasis,
                        cudaMemcpyHostToDevice, s));
+  if (wt)
+    CK(cudaMemcpyAsync(dw, opt.price_weight, sizeof(float) * p->extw, cudaMemcpyHostToDevice,
+                       s));
   CK(cudaMemcpyAsync(dA, bt->A, sizeof(double) * p->extA, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(db, bt->b, sizeof(double) * p->extb, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(dc, bt->c, sizeof(double) * p->extc, cudaMemcpyHostToDevice, s));
-  if ((rc = blpg_plan_execute(p, dA, db, dc, dhint, &dres, s))) return rc;
+  if ((rc = blpg_plan_execute_weighted(p, dA, db, dc, dhint, dw, &dres, s))) return rc;
   CK(cudaMemcpyAsync(out->status, dres.status, sizeof(int32_t) * N, cudaMemcpyDeviceToHost,
                      s));
   CK(cudaMemcpyAsync(out->objective, dres.objective, sizeof(double) * N,

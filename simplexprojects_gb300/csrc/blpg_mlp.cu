@@ -233,6 +233,21 @@ __global__ void build_features(int count, int m, int n, int F, const int64_t* __
 
 // Top-m selection: the m highest-scoring of n + m columns of LP k, in
 // decreasing score order (ties by lower column), written as its basis hint.
+// Steepest-edge weights from scores: w_j = 1 + beta * sigmoid(score_j) for
+// the n[k] + m[k] columns of LP k (one CTA per LP).
+__global__ void price_weights(const float* __restrict__ scores, int lds, int count,
+                              const int32_t* __restrict__ d_m, const int32_t* __restrict__ d_n,
+                              const int64_t* __restrict__ offw, float beta,
+                              float* __restrict__ w) {
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  const int cols = d_n[k] + d_m[k];
+  const float* sk = scores + (size_t)k * lds;
+  float* wk = w + offw[k];
+  for (int j = threadIdx.x; j < cols; j += blockDim.x)
+    wk[j] = 1.f + beta / (1.f + expf(-sk[j]));
+}
+
 __global__ void __launch_bounds__(512) topm(const float* __restrict__ scores, int lds, int count,
                                             const int32_t* __restrict__ mm,
                                             const int32_t* __restrict__ nn,
@@ -586,6 +601,19 @@ extern "C" int32_t blpg_features(int32_t count, int32_t m, int32_t n, int32_t fa
     return blpg::fail(BLPG_EINVAL, "blpg_features: bad arguments");
   build_features<<<count, 128, 0, (cudaStream_t)stream>>>(count, m, n, families, d_offb, d_offc,
                                                           db, dc, d_family, d_mean, d_std, dX, ldx);
+  MCK(cudaGetLastError());
+  return BLPG_OK;
+}
+
+extern "C" int32_t blpg_price_weights(const float* d_scores, int32_t lds, int32_t count,
+                                      const int32_t* d_m, const int32_t* d_n, int32_t max_cols,
+                                      const int64_t* d_offw, float beta, float* d_weight,
+                                      void* stream) {
+  if (count <= 0) return BLPG_OK;
+  if (!d_scores || !d_m || !d_n || !d_offw || !d_weight || max_cols < 1 || lds < max_cols)
+    return blpg::fail(BLPG_EINVAL, "blpg_price_weights: bad arguments");
+  price_weights<<<count, 128, 0, (cudaStream_t)stream>>>(d_scores, lds, count, d_m, d_n, d_offw,
+                                                         beta, d_weight);
   MCK(cudaGetLastError());
   return BLPG_OK;
 }

@@ -92,7 +92,7 @@ int32_t run(int32_t count, int32_t max_m, int32_t max_n, const blpg::dev::LpArgs
   if (!K)
     return fail(BLPG_ETOOBIG, "blpg_solve_noalloc: m=%d n=%d exceeds an 8-CTA cluster", max_m,
                 max_n);
-  ClassArgs ca;
+  ClassArgs ca{};
   ca.order = scratch + kOrderOffset;
   ca.count = count;
   ca.ticket = scratch;
@@ -101,6 +101,7 @@ int32_t run(int32_t count, int32_t max_m, int32_t max_n, const blpg::dev::LpArgs
   ca.max_ldw = ldw;
   ca.max_na = 0;
   ca.max_nv = max_n + max_m;
+  ca.se = 0;  // Dantzig pricing: no column norms
   noalloc_reset<<<(count + 255) / 256 > 0 ? (count + 255) / 256 : 1, 256, 0, s>>>(scratch, count);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)

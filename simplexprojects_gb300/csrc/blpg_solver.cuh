@@ -79,6 +79,9 @@ struct LpArgs {
   int32_t refresh_period;  // FP32: FP64 refresh every k pivots (0: at the end)
   int32_t warm_mode;       // 0: hinted basis infeasible both ways -> cold; 1: cost-shifted dual
   double shift;            // cost shift of warm_mode 1
+  int32_t pricing;         // 0: Dantzig, 1: steepest edge (exact column norms)
+  const float* weight;     // nullable: steepest-edge score weight per variable (n + m per LP)
+  const int64_t* offw;     // offsets of `weight`
 };
 
 // Bits of the per-LP info output.
@@ -99,6 +102,7 @@ struct ClassArgs {
   int32_t max_ldw;
   int32_t max_na;   // artificial columns (two-phase LPs)
   int32_t max_nv;   // variables n + m + na
+  int32_t se;       // steepest-edge pricing: the layout holds column norms
 };
 
 template <typename T>
@@ -137,8 +141,8 @@ struct Geom {
 
 // Shared-memory layout of a class (bytes).  Identical on host and device.
 struct Layout {
-  int tab, colA, colB, rhsx, basis, flags, cvar, vpos, ext, red, state, total;
-  __host__ __device__ Layout(int max_m, int max_ldw, int max_nv, int elem) {
+  int tab, colA, colB, rhsx, basis, flags, cvar, vpos, ext, red, state, gam, total;
+  __host__ __device__ Layout(int max_m, int max_ldw, int max_nv, int elem, int se = 0) {
     int mp1 = round_up(max_m + 1, 4);
     int nvp = round_up(max_nv, 4);
     tab = 0;
@@ -159,7 +163,21 @@ struct Layout {
     off += nvp * 4;
     ext = off;
     // FP32 tableau: FP64 x_B and duals of the refresh, FP32 residual copy
-    if (elem == 4) off += 2 * mp1 * 8 + mp1 * 4;
+    const int ext_bytes = elem == 4 ? 2 * mp1 * 8 + mp1 * 4 : 0;
+    off += ext_bytes;
+    // steepest edge: one 64-bit fixed-point norm per local column slot,
+    // sharing the refresh's region when it is large enough (the norms are
+    // recomputed after every refresh)
+    gam = -1;
+    if (se) {
+      if (ext_bytes >= max_ldw * 8) {
+        gam = ext;
+      } else {
+        off = round_up(off, 16);
+        gam = off;
+        off += round_up(max_ldw * 8, 16);
+      }
+    }
     red = off;
     off += 3 * 32 * 16;  // three argmin scratch buffers (pricing, ratio, Harris)
     state = off;
@@ -290,12 +308,33 @@ __device__ __forceinline__ float4 v_fma(float f, const float4& p, const float4& 
   return make_float4(fmaf(-f, p.x, t.x), fmaf(-f, p.y, t.y), fmaf(-f, p.z, t.z),
                      fmaf(-f, p.w, t.w));
 }
+__device__ __forceinline__ double2 v_sq(const double2& t, const double2& a) {
+  return make_double2(fma(t.x, t.x, a.x), fma(t.y, t.y, a.y));
+}
+__device__ __forceinline__ float4 v_sq(const float4& t, const float4& a) {
+  return make_float4(fmaf(t.x, t.x, a.x), fmaf(t.y, t.y, a.y), fmaf(t.z, t.z, a.z),
+                     fmaf(t.w, t.w, a.w));
+}
 __device__ __forceinline__ double2 v_div(const double2& a, double d) {
   return make_double2(a.x / d, a.y / d);
 }
 __device__ __forceinline__ float4 v_div(const float4& a, float d) {
   return make_float4(__fdiv_rn(a.x, d), __fdiv_rn(a.y, d), __fdiv_rn(a.z, d),
                      __fdiv_rn(a.w, d));
+}
+
+// Steepest-edge column norms are summed as 64-bit fixed-point integers with
+// 2^-24 resolution (shared-memory atomics; integer sums do not depend on the
+// order of the additions).  gamma_j = 1 + sum_i T_ij^2.  A partial sum is
+// clamped to 2^30 so that no total can overflow.
+__device__ __forceinline__ unsigned long long norm_fixed(float v) {
+  return __float2ull_rn(fminf(v, 1073741824.f) * 16777216.f);
+}
+__device__ __forceinline__ unsigned long long norm_fixed(double v) {
+  return __double2ull_rn(fmin(v, 1073741824.0) * 16777216.0);
+}
+__device__ __forceinline__ double norm_value(unsigned long long u) {
+  return 1.0 + (double)u * (1.0 / 16777216.0);
 }
 
 // Status codes (GLPK numbering, as blpg.h)
@@ -333,6 +372,7 @@ struct Solver {
   int* flags;
   int* cvar;   // slot -> variable id (every slot of the LP, replicated per CTA)
   int* vpos;   // variable -> slot if nonbasic, -1 - row if basic
+  unsigned long long* gam;  // steepest edge: fixed-point column norms of the local slots
   double* xr;  // FP32 tableau only: FP64 x_B of the refresh
   double* yr;  // FP32 tableau only: FP64 duals of the refresh
   float* rf;   // FP32 tableau only: the refresh's residuals rounded to FP32
@@ -511,19 +551,27 @@ struct Solver {
   // extracts its column into colx_next, every CTA extracts its RHS replica.
   __device__ void update_body(const Geom& g, int r, int s, const T* pcol, int sn, int owner_n,
                               int c0, T* colx_next) {
-    update_rows(tab, rhsx, rank, g.m, g.ldw, g.nl, g.cw, r, s, pcol, sn, owner_n, c0,
-                colx_next);
+    update_rows<false>(tab, rhsx, rank, g.m, g.ldw, g.nl, g.cw, r, s, pcol, sn, owner_n, c0,
+                       colx_next, nullptr, 0);
+  }
+  // The same sweep, also summing the squares of every row's final values
+  // into the column norms (steepest-edge pricing).
+  __device__ void update_body_se(const Geom& g, int r, int s, const T* pcol, int c0, int lc) {
+    update_rows<true>(tab, rhsx, rank, g.m, g.ldw, g.nl, g.cw, r, s, pcol, -1, -1, c0, nullptr,
+                      gam, lc);
   }
   // Kept out of line with plain arguments (no `this`, no structs by
   // reference) so that the unrolled sweep has its own register budget and
   // nothing in its loop lives in local memory.  The slot s entry of every
   // updated row is taken as 0 before the elimination (it held the entering
   // column, whose slot now carries the leaving variable's unit column).
+  template <bool SE>
   static __device__ __noinline__ void update_rows(T* const tb, T* const rhsx, const int rank,
                                                   const int m, const int ldw, const int nl,
                                                   const int cw, const int r, const int s,
                                                   const T* pcol, const int qn, const int owner_n,
-                                                  const int c0, T* colx_next) {
+                                                  const int c0, T* colx_next,
+                                                  unsigned long long* gam, const int lc) {
     const int nt = (int)blockDim.x;
     const int G = nt / nl;
     const int grp = threadIdx.x / nl;
@@ -541,6 +589,7 @@ struct Solver {
     // grp + G, ... are disjoint, so this only adds parallelism).  Row r
     // already holds the divided pivot row and is only read.
     constexpr int kU = 2;
+    VT sq = VT{};  // steepest edge: sum of squares of this lane's final values
     int i0 = grp;
     for (; i0 + (kU - 1) * G < m; i0 += kU * G) {
       T f[kU];
@@ -561,6 +610,7 @@ struct Solver {
         }
         if (has_q) colx_next[i] = vget<VT, T>(t[u], qe);
         if (has_rhs) rhsx[i] = vget<VT, T>(t[u], 0);
+        if (SE) sq = v_sq(t[u], sq);
       }
     }
     for (; i0 < m; i0 += G) {
@@ -573,6 +623,14 @@ struct Solver {
       }
       if (has_q) colx_next[i0] = vget<VT, T>(t, qe);
       if (has_rhs) rhsx[i0] = vget<VT, T>(t, 0);
+      if (SE) sq = v_sq(t, sq);
+    }
+    if (SE) {
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        const int lj = lane * V + e;
+        if (lj < lc) atomicAdd(&gam[lj], norm_fixed(vget<VT, T>(sq, e)));
+      }
     }
     if (has_q && grp == 0) colx_next[m] = tb[(size_t)m * ldw + qloc];
   }
@@ -646,6 +704,124 @@ struct Solver {
       q = qn;
       s = sn;
       owner = owner_n;
+    }
+  }
+
+  // ---- steepest-edge pricing --------------------------------------------
+  // Column norms gamma_j = 1 + sum_{i<m} T_ij^2 of the current tableau,
+  // recomputed with a full pass (at the start of a pricing loop, after
+  // loads, crashes, refreshes and pivots made without norms).
+  __device__ void norms_full(const Geom& g, int lc) {
+    for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = 0ull;
+    __syncthreads();
+    const int nt = (int)blockDim.x, G = nt / g.nl;
+    const int grp = threadIdx.x / g.nl, lane = threadIdx.x - grp * g.nl;
+    if (grp < G) {
+      VT sq = VT{};
+      for (int i = grp; i < g.m; i += G)
+        sq = v_sq(*reinterpret_cast<const VT*>(tab + (size_t)i * g.ldw + lane * V), sq);
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        const int lj = lane * V + e;
+        if (lj < lc) atomicAdd(&gam[lj], norm_fixed(vget<VT, T>(sq, e)));
+      }
+    }
+    __syncthreads();
+  }
+
+  // Steepest-edge pricing: among d_j < -opt_tol (variables below
+  // price_cols), the largest d_j^2 / gamma_j, times weight[j] when weights
+  // are given; ties to the lowest variable id.  Bland's rule (after a
+  // degenerate streak) takes the lowest eligible id as in Dantzig mode.
+  __device__ Key price_se(const Geom& g, int c0, int lc, bool bland, T opt_tol, int price_cols,
+                          const float* w) {
+    Key k = key_none();
+    const T* d = tab + (size_t)g.m * g.ldw;
+    for (int lj = threadIdx.x; lj < lc; lj += blockDim.x) {
+      const int j = cvar[c0 + lj];
+      const T v = d[lj];
+      if (j < price_cols && v < -opt_tol) {
+        Key kk;
+        if (bland) {
+          kk = price_key(v, j, c0 + lj, true);
+        } else {
+          const unsigned long long u = gam[lj];
+          const float gm =
+              1.f + ((float)(unsigned)(u >> 32) * 4294967296.f + (float)(unsigned)u) *
+                        (1.f / 16777216.f);
+          const float vf = (float)v;
+          float sc = __fdividef(vf * vf, gm);
+          if (w) sc *= w[j];
+          kk = Key{~__float_as_uint(sc), 0u, (unsigned)j, (unsigned)(c0 + lj)};
+        }
+        if (key_less(kk, k)) k = kk;
+      }
+    }
+    k = block_min(k, redP);
+    return cluster_min(k);
+  }
+
+  // The primal loop with the plan's pricing rule over variables < n + m.
+  __device__ int primal(const Geom& g, int c0, int lc, const LpArgs& a, const float* w,
+                        int max_piv, int& pivots, bool& bland, int& degen, int& cur,
+                        int period = 0) {
+    if (a.pricing == 1 && gam)
+      return loop_se(g, c0, lc, g.n + g.m, a, w, max_piv, pivots, bland, degen, cur, period);
+    return loop(g, c0, lc, g.n + g.m, a, max_piv, pivots, bland, degen, cur, period);
+  }
+
+  // The primal loop with steepest-edge pricing.  Pricing needs the norms of
+  // the updated tableau, so it runs after the sweep (which sums them), and
+  // the entering column is then extracted by its owner.
+  __device__ int loop_se(const Geom& g, int c0, int lc, int price_cols, const LpArgs& a,
+                         const float* w, int max_piv, int& pivots, bool& bland, int& degen,
+                         int& cur, int period = 0) {
+    const T opt_tol = (T)a.opt_tol, piv_tol = (T)a.piv_tol, feas_tol = (T)a.feas_tol;
+    const T deg_tol = (T)a.deg_tol;
+    norms_full(g, lc);
+    for (;;) {
+      Key kq = price_se(g, c0, lc, bland, opt_tol, price_cols, w);
+      const int q = kq.w2 == ~0u ? -1 : (int)kq.w2;
+      if (q < 0) return kOpt;
+      if (pivots >= max_piv) return kUndef;
+      const int s = (int)kq.w3;
+      const int owner = s / g.cw;
+      if (owner == rank) extract(g, s, c0, colbuf(cur));
+      if (CLUSTER) {
+        csync();
+        if (owner != rank) {
+          // the column from its owner, the RHS from this CTA's own replica
+          // (replicas are bit-identical, so every CTA's ratio test agrees)
+          const T* src = remote(colbuf(cur), owner);
+          for (int i = threadIdx.x; i <= g.m; i += blockDim.x) {
+            colbuf(cur)[i] = src[i];
+            rhsx[i] = tab[(size_t)i * g.ldw + g.cw];
+          }
+        }
+      }
+      __syncthreads();
+      // the norms are summed afresh by this pivot's sweep (the pricing
+      // reads above are done: barriers since)
+      for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = 0ull;
+      // ratio test: every CTA holds the column, so each computes it
+      T theta = T(0);
+      Key kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta);
+      const int r = kr.w2 == ~0u ? -1 : (int)kr.w3;
+      if (r < 0) return kUnbnd;
+      if (theta <= deg_tol) {
+        if (++degen > a.bland_after) bland = true;
+      } else {
+        degen = 0;
+      }
+      const T* pcol = colbuf(cur);
+      const int lv = basis[r];
+      pivot_rows(g, r, s, lv, pcol, c0, lc, false, T(0), 0);
+      relabel(r, s, q, lv);
+      update_body_se(g, r, s, pcol, c0, lc);
+      __syncthreads();
+      ++pivots;
+      if (pivots >= max_piv) return kUndef;
+      if (period > 0 && pivots % period == 0) return kRefresh;
     }
   }
 
@@ -1328,13 +1504,14 @@ struct Solver {
       const int lc = max(0, min(g.cw, g.Wc - c0));
       load(g, c0, lc, A, b, c);
       int pivots = 0, degen = 0, cur = 0, st, info = 0;
+      const float* w = a.weight ? a.weight + a.offw[lp] : nullptr;
       bool bland = false, refreshed = false;
       const int max_piv = a.max_pivots > 0 ? a.max_pivots : 50 * (m + n) + 1000;
       const T ptol = (T)a.ptol, opt_tol = (T)a.opt_tol;
       if (na > 0) {
         objective_row(g, c0, lc, c, true);
         __syncthreads();
-        st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
+        st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
         if (CLUSTER) csync();
         if (st == kOpt) {
           const double z = (double)tab[(size_t)m * g.ldw + g.cw];
@@ -1348,7 +1525,7 @@ struct Solver {
           __syncthreads();
           bland = false;
           degen = 0;
-          st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
+          st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
         }
       } else {
         st = -1;
@@ -1359,11 +1536,11 @@ struct Solver {
           // (the final FP64 refresh verifies whatever basis the finish ends on)
           const int fl = check_feasible(g, c0, lc, ptol, opt_tol);
           if (fl & 1) {
-            st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
+            st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
           } else if (fl & 2) {
             info |= kInfoDual;
             st = dual_loop(g, c0, lc, a, max_piv, pivots, cur, ptol);
-            if (st == kOpt) st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
+            if (st == kOpt) st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
           } else if (a.warm_mode == 1) {
             // infeasible both ways: shift the costs of the columns with
             // d_j < -opt_tol to small distinct positive values (dual
@@ -1381,7 +1558,7 @@ struct Solver {
             if (st == kOpt) {
               objective_row(g, c0, lc, c, false);
               __syncthreads();
-              st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
+              st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
             }
           }
           if (st < 0 || st == kNoFeas) {
@@ -1398,7 +1575,7 @@ struct Solver {
         if (st < 0) {
           const int period = kFP32 ? a.refresh_period : 0;
           for (;;) {
-            st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur, period);
+            st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur, period);
             if (st != kRefresh) break;
             if (CLUSTER) csync();
             refresh(g, A, b, c, a);
@@ -1420,7 +1597,7 @@ struct Solver {
               st = dual_loop(g, c0, lc, a, max_piv, pivots, cur, ptol);
               if (st != kOpt) break;
             }
-            st = loop(g, c0, lc, n + m, a, max_piv, pivots, bland, degen, cur);
+            st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
             if (st != kOpt) break;
           }
         }
@@ -1469,7 +1646,7 @@ template <typename T, bool CLUSTER>
 __global__ void __launch_bounds__(512, 1) solve_kernel(const LpArgs a, const ClassArgs ca) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Solver<T, CLUSTER> s;
-  const Layout L(ca.max_m, ca.max_ldw, ca.max_nv, (int)sizeof(T));
+  const Layout L(ca.max_m, ca.max_ldw, ca.max_nv, (int)sizeof(T), ca.se);
   s.smem = smem_raw;
   s.tab = reinterpret_cast<T*>(smem_raw + L.tab);
   s.col0 = reinterpret_cast<T*>(smem_raw + L.colA);
@@ -1482,6 +1659,7 @@ __global__ void __launch_bounds__(512, 1) solve_kernel(const LpArgs a, const Cla
   s.xr = reinterpret_cast<double*>(smem_raw + L.ext);
   s.yr = s.xr + round_up(ca.max_m + 1, 4);
   s.rf = reinterpret_cast<float*>(s.yr + round_up(ca.max_m + 1, 4));
+  s.gam = L.gam >= 0 ? reinterpret_cast<unsigned long long*>(smem_raw + L.gam) : nullptr;
   s.redP = reinterpret_cast<Key*>(smem_raw + L.red);
   s.redR = s.redP + 32;
   s.redH = s.redP + 64;

@@ -30,13 +30,20 @@ class SolveResult:
     info: Optional[np.ndarray] = None
 
 
+PRICING = {"dantzig": 0, "steepest": 1}
+
+
 def options(precision: str = "fp64", **kw) -> N.Options:
+    """blpg_options for `precision` ("fp64" | "fp32"); keyword arguments set
+    fields by name (pricing also takes "dantzig" | "steepest")."""
     o = N.Options()
     N.lib().blpg_options_init(C.byref(o))
     o.precision = PRECISIONS[precision]
     for k, v in kw.items():
         if v is None:
             continue
+        if k == "pricing" and isinstance(v, str):
+            v = PRICING[v]
         if not hasattr(o, k):
             raise TypeError(f"unknown option {k}")
         setattr(o, k, v)
@@ -44,9 +51,12 @@ def options(precision: str = "fp64", **kw) -> N.Options:
 
 
 def solve(batch: LPBatch, precision: str = "fp64", want_x: bool = False,
-          want_basis: bool = False, hint: Optional[np.ndarray] = None, **opts) -> SolveResult:
+          want_basis: bool = False, hint: Optional[np.ndarray] = None,
+          weight: Optional[np.ndarray] = None, **opts) -> SolveResult:
     """Solve every LP of a host batch on the GPU (blocking).  `hint` (optional)
-    is a packed array of m[k] basic column ids per LP (a warm-start basis)."""
+    is a packed array of m[k] basic column ids per LP (a warm-start basis);
+    `weight` (optional, with pricing="steepest") n[k] + m[k] score factors
+    per LP, packed."""
     L = N.lib()
     k = batch.count
     st = np.zeros(k, np.int32)
@@ -64,6 +74,11 @@ def solve(batch: LPBatch, precision: str = "fp64", want_x: bool = False,
         if hint.size != int(batch.m.sum()):
             raise ValueError("hint must hold m[k] column ids per LP")
         o.basis_hint = N.ptr(hint, C.c_int32)
+    if weight is not None:
+        weight = np.ascontiguousarray(weight, dtype=np.float32)
+        if weight.size != int((batch.n + batch.m).sum()):
+            raise ValueError("weight must hold n[k] + m[k] factors per LP")
+        o.price_weight = N.ptr(weight, C.c_float)
     bst = batch.c_struct()
     N.check(L.blpg_solve_batch(C.byref(bst), C.byref(o), C.byref(res)), "blpg_solve_batch")
     return SolveResult(st, ob, pv, x, bs, info)
@@ -108,14 +123,15 @@ class Plan:
 
     def execute(self, dA: int, db: int, dc: int, status: int, objective: int, x: int = 0,
                 pivots: int = 0, basis: int = 0, stream: int = 0, basis_hint: int = 0,
-                info: int = 0) -> None:
+                info: int = 0, weight: int = 0) -> None:
         """Enqueue a solve on raw device pointers (ints) on `stream`."""
         res = N.Result(C.cast(status, N.i32p), C.cast(objective, N.f64p),
                        C.cast(x, N.f64p) if x else None, C.cast(pivots, N.i32p) if pivots else None,
                        C.cast(basis, N.i32p) if basis else None,
                        C.cast(info, N.i32p) if info else None)
-        N.check(self._L.blpg_plan_execute(self._h, dA, db, dc, basis_hint or None,
-                                          C.byref(res), stream or None), "blpg_plan_execute")
+        N.check(self._L.blpg_plan_execute_weighted(self._h, dA, db, dc, basis_hint or None,
+                                                   weight or None, C.byref(res), stream or None),
+                "blpg_plan_execute")
 
     def close(self):
         if self._h:
@@ -154,9 +170,10 @@ class DeviceBatch:
                       if want_basis else None)
         self.info = torch.zeros(k, dtype=torch.int32, device=dev)
 
-    def run(self, stream=None, hint=None) -> None:
+    def run(self, stream=None, hint=None, weight=None) -> None:
         """Enqueue one solve; `hint` is an optional int32 CUDA tensor of m[k]
-        basic column ids per LP (a warm-start basis)."""
+        basic column ids per LP (a warm-start basis), `weight` an optional
+        float32 CUDA tensor of n[k] + m[k] steepest-edge score factors per LP."""
         torch = self.torch
         s = stream if stream is not None else torch.cuda.current_stream()
         self.plan.execute(self.A.data_ptr(), self.b.data_ptr(), self.c.data_ptr(),
@@ -166,7 +183,8 @@ class DeviceBatch:
                           self.basis.data_ptr() if self.basis is not None else 0,
                           stream=s.cuda_stream,
                           basis_hint=hint.data_ptr() if hint is not None else 0,
-                          info=self.info.data_ptr())
+                          info=self.info.data_ptr(),
+                          weight=weight.data_ptr() if weight is not None else 0)
 
     def result(self) -> SolveResult:
         self.torch.cuda.synchronize()

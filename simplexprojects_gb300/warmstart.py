@@ -227,6 +227,29 @@ class WarmStart:
                 "blpg_topm_hint")
         return hint_out
 
+    def weights_launches(self, count: int) -> int:
+        """Kernels one predict_weights() over `count` LPs launches."""
+        return 1 + self.mlp.predict_launches((count + 63) // 64 * 64) + 1
+
+    def predict_weights(self, d, m_dev, n_dev, offw_dev, w_out=None, stream=None, scratch=None,
+                        beta: float = 1.0):
+        """Steepest-edge score factors 1 + beta * p_j (p_j the network's
+        probability that column j is basic), n + m per LP, for a device batch."""
+        torch = self.torch
+        X = self.features(d, out=scratch.get("X") if scratch else None, stream=stream)
+        rows = X.shape[0]
+        logits = (scratch.get("logits") if scratch else None)
+        if logits is None:
+            logits = torch.empty((rows, self.mlp.d_out_pad), dtype=torch.float32, device=self.dev)
+        self.mlp.predict(X, logits, stream)
+        if w_out is None:
+            w_out = torch.empty(d["count"] * self.nf, dtype=torch.float32, device=self.dev)
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        N.check(N.lib().blpg_price_weights(_vp(logits), self.mlp.d_out_pad, d["count"], _vp(m_dev),
+                                           _vp(n_dev), self.nf, _vp(offw_dev), float(beta),
+                                           _vp(w_out), s), "blpg_price_weights")
+        return w_out
+
     # ---- checkpoints ------------------------------------------------------
     def save(self, path: str) -> None:
         """Parameters (binary FP32) and a JSON header with the dimensions and
@@ -263,17 +286,33 @@ def basis_accuracy(pred: np.ndarray, truth: np.ndarray, m: int):
 class LearnedSolver:
     """Solve batches of one LP shape with the learned warm start.
 
-    ``run()`` enqueues features -> network -> top-m hint -> hinted solve on
+    Two ways of using the network:
+      mode="guided" (default): the slack-basis primal simplex with
+        steepest-edge pricing whose scores are multiplied by 1 + p_j, p_j
+        the network's probability that column j is basic in the optimum;
+      mode="crash": the m most probable columns as a basis hint, pivoted in
+        and finished by primal, dual or cost-shifted dual simplex (cold
+        solve as the fallback), with the plan's pricing (Dantzig unless
+        ``pricing="steepest"`` is passed).
+
+    ``run()`` enqueues features -> network -> weights or hint -> solve on
     device-resident data (the plan's CUDA graph for the solve);
     ``solve(batch)`` is the end-to-end call from host arrays (copies of A, b,
     c in, status / objective / pivots out)."""
 
-    def __init__(self, ws: WarmStart, batch: LPBatch, precision: str = "fp32", **opts):
+    def __init__(self, ws: WarmStart, batch: LPBatch, precision: str = "fp32",
+                 mode: str = "guided", beta: float = 1.0, **opts):
         import torch
         from .solver import DeviceBatch
+        if mode not in ("guided", "crash"):
+            raise ValueError("mode must be 'guided' or 'crash'")
         self.torch = torch
         self.ws = ws
         self.batch = batch
+        self.mode = mode
+        self.beta = beta
+        if mode == "guided":
+            opts["pricing"] = "steepest"
         self.db = DeviceBatch(batch, precision, device=str(ws.dev), **opts)
         self.d = ws.device_inputs(batch)
         # the feature kernel and the solver read the same b, c buffers
@@ -283,19 +322,36 @@ class LearnedSolver:
         self.n_dev = torch.from_numpy(batch.n).to(ws.dev)
         offh = np.concatenate([[0], np.cumsum(batch.m.astype(np.int64))[:-1]]).astype(np.int64)
         self.offh_dev = torch.from_numpy(offh).to(ws.dev)
+        nm = (batch.n + batch.m).astype(np.int64)
+        offw = np.concatenate([[0], np.cumsum(nm)[:-1]]).astype(np.int64)
+        self.offw_dev = torch.from_numpy(offw).to(ws.dev)
         self.hint = torch.empty(int(batch.m.sum()), dtype=torch.int32, device=ws.dev)
+        self.weight = torch.empty(int(nm.sum()), dtype=torch.float32, device=ws.dev)
         rows = (k + 63) // 64 * 64
         self.scratch = dict(
             X=torch.zeros((rows, ws.mlp.d_in_pad), dtype=torch.float32, device=ws.dev),
             logits=torch.empty((rows, ws.mlp.d_out_pad), dtype=torch.float32, device=ws.dev))
 
     def predict(self, stream=None):
+        if self.mode == "guided":
+            return self.ws.predict_weights(self.d, self.m_dev, self.n_dev, self.offw_dev,
+                                           self.weight, stream, self.scratch, self.beta)
         return self.ws.predict_hint(self.d, self.m_dev, self.n_dev, self.offh_dev, self.hint,
                                     stream, self.scratch)
 
+    def launches(self) -> int:
+        """Kernels one run() launches."""
+        k = self.batch.count
+        pred = (self.ws.weights_launches(k) if self.mode == "guided"
+                else self.ws.hint_launches(k))
+        return pred + self.db.plan.launches()
+
     def run(self, stream=None) -> None:
         self.predict(stream)
-        self.db.run(stream, hint=self.hint)
+        if self.mode == "guided":
+            self.db.run(stream, weight=self.weight)
+        else:
+            self.db.run(stream, hint=self.hint)
 
     def result(self):
         return self.db.result()

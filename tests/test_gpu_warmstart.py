@@ -100,7 +100,7 @@ def test_learned_warm_start_end_to_end(built):
     rep = ws.train(train, tb.basis, epochs=16, lr=1e-3)
     assert rep.losses[-1] < rep.losses[0]
     cold = sp.solve(held, "fp64", want_basis=True)
-    ls = LearnedSolver(ws, held, "fp64")
+    ls = LearnedSolver(ws, held, "fp64", mode="crash")
     ls.run()
     res = ls.result()
     hint = ls.hint.cpu().numpy()
@@ -112,12 +112,33 @@ def test_learned_warm_start_end_to_end(built):
     orc = ref.solve_batch(held, "fp64", hint=hint)
     assert np.array_equal(res.pivots, orc.pivots) and np.array_equal(res.info, orc.info)
     assert np.array_equal(res.objective.view(np.uint64), orc.objective.view(np.uint64))
-    l32 = LearnedSolver(ws, held, "fp32")
+    l32 = LearnedSolver(ws, held, "fp32", mode="crash")
     r32 = l32.solve(held)
     assert np.array_equal(r32.status, cold.status)
     opt = cold.status == 5
     rel = np.abs(r32.objective[opt] - cold.objective[opt]) / np.abs(cold.objective[opt])
     assert rel.max() <= 1e-6
+    # guided mode: the network's probabilities weight steepest-edge pricing.
+    # Against the same pricing without the network: fewer pivots.
+    cold_se = sp.solve(held, "fp64", pricing="steepest")
+    lg = LearnedSolver(ws, held, "fp64", mode="guided")
+    lg.run()
+    rg = lg.result()
+    assert np.array_equal(rg.status, cold.status)
+    assert _relerr(rg.objective[opt], cold.objective[opt]) <= 1e-9
+    assert rg.pivots.mean() < 0.95 * cold_se.pivots.mean()
+    w = lg.weight.cpu().numpy()
+    assert w.min() >= 1.0 and w.max() <= 2.0
+    orc = ref.solve_batch(held, "fp64", pricing="steepest", weight=w)
+    assert np.array_equal(orc.status, cold.status)
+    assert abs(rg.pivots.mean() - orc.pivots.mean()) <= 0.05 * orc.pivots.mean()
+    g32 = LearnedSolver(ws, held, "fp32", mode="guided").solve(held)
+    assert np.array_equal(g32.status, cold.status)
+    assert _relerr(g32.objective[opt], cold.objective[opt]) <= 1e-6
+
+
+def _relerr(a, b):
+    return float((np.abs(a - b) / np.maximum(np.abs(b), 1.0)).max()) if a.size else 0.0
 
 
 def test_warm_start_checkpoint_roundtrip(built, tmp_path):
