@@ -77,7 +77,7 @@ static int device_check(int device, cudaDeviceProp* prop) {
 }
 
 struct ClassPlan {
-  int K = 1, nt = 128, max_m = 0, max_ldw = 0, max_na = 0, max_nv = 0, smem = 0;
+  int K = 1, nt = 128, max_m = 0, max_na = 0, smem = 0;
   int ctas_per_sm = 1;
   int count = 0, grid = 0, order_off = 0;
   double work = 0;
@@ -218,29 +218,33 @@ static int pick_threads(const blpg_plan* p, int nl, int smem, int regs, int K, i
   return std::min(dev::round_up(nl, 32), kMaxThreads);
 }
 
-// Size classes.  Every LP gets the smallest cluster size K whose per-CTA
-// layout fits the CTA shared-memory budget (default: two CTAs per SM), so
-// large tableaux are spread over more SMs (shorter critical path) and all
-// classes have the same per-SM footprint.  One class per K; classes run
-// concurrently, each with a grid proportional to its share of the work.
+// Size classes.  Every LP gets the smallest cluster size K whose layout fits
+// the CTA shared-memory budget (default: the whole per-CTA shared memory,
+// i.e. the fewest CTAs per LP).  LPs that need a cluster form one class per
+// K; single-CTA LPs are grouped by how many CTAs of their own layout fit an
+// SM (1..16, capped by the tuning table's "fpXX_ctas"), so small LPs run
+// many per SM.  A CTA lays out each LP it takes in its own allocation, so a
+// class needs only its largest member's layout and never splits.  Every
+// class is launched with a full-residency grid, heaviest LPs first: the
+// classes overlap on the GPU as earlier classes' persistent CTAs run out of
+// work, which balances them without a work estimate.
 template <typename T>
 static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
   constexpr int V = dev::VecT<T>::V;
   const int elem = (int)sizeof(T);
   int budget = p->opt.cta_smem_budget;
-  if (budget <= 0) {
-    std::lock_guard<std::mutex> lk(g_tuning.mu);
-    auto it = g_tuning.threads.find({p->precision * 16 + 15, 1});
-    // default: the whole per-CTA shared memory, i.e. the fewest CTAs per LP
-    // (measured on GB300: cluster barriers and DSMEM exchanges cost more
-    // than the occupancy they buy)
-    budget = it != g_tuning.threads.end() ? it->second : max_smem;
-  }
+  if (budget <= 0) budget = tuning_value(p->precision * 16 + 15, 1, max_smem);
   budget = std::min(budget, max_smem);
   const int se = p->opt.pricing == BLPG_PRICE_STEEPEST ? 1 : 0;
   const int min_cluster = std::max(1, std::min(p->opt.min_cluster, max_cluster));
+  constexpr int kMaxCtasPerSm = 16;
+  const int cps_cap =
+      std::max(1, std::min(kMaxCtasPerSm, tuning_value(p->precision * 16 + 14, 2, kMaxCtasPerSm)));
+  auto cta_limit = [&](int cps) {  // per-CTA shared memory for cps CTAs per SM
+    return std::min(max_smem, p->smem_per_sm / cps - p->smem_reserved);
+  };
   struct Item {
-    int K, nl, ldw, nv;
+    int K, nl, bytes;
     double work;
   };
   std::vector<Item> items(p->count);
@@ -251,11 +255,10 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
       const int lim = pass == 0 ? budget : max_smem;
       for (int K = min_cluster; K <= max_cluster; K *= 2) {
         Geom g(m, n, na, K, V);
-        const int nv = n + m + na;
-        if (Layout(m, g.ldw, nv, elem, se).total <= lim && g.nl <= kMaxThreads) {
+        const int bytes = Layout(m, g.ldw, n + m + na, elem, se).total;
+        if (bytes <= lim && g.nl <= kMaxThreads) {
           chosen = K;
-          items[k] = {K, g.nl, g.ldw, nv,
-                      (double)(m + 1) * (double)(n + na + 1) * (double)(m + n)};
+          items[k] = {K, g.nl, bytes, (double)(m + 1) * (double)(n + na + 1) * (double)(m + n)};
           break;
         }
       }
@@ -265,80 +268,59 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
                   "LP %d (m=%d, n=%d) needs more than %d CTAs of shared memory", k, m,
                   n, max_cluster);
   }
-  std::map<int, std::vector<int>> groups;
-  for (int k = 0; k < p->count; ++k) groups[items[k].K].push_back(k);
+  std::map<int, std::vector<int>> groups;  // key: 100 + K for clusters, else CTAs per SM
+  for (int k = 0; k < p->count; ++k) {
+    int key = 100 + items[k].K;
+    if (items[k].K == 1) {
+      int cps = std::max(1, std::min(cps_cap, p->smem_per_sm / (items[k].bytes + p->smem_reserved)));
+      while (cps > 1 && items[k].bytes > cta_limit(cps)) --cps;
+      key = cps;
+    }
+    groups[key].push_back(k);
+  }
   p->classes.clear();
   p->order.clear();
-  double total_work = 0;
-  for (auto& it : items) total_work += it.work;
+  std::vector<std::pair<ClassPlan, std::vector<int>>> built;
   for (auto& kv : groups) {
     auto& lps = kv.second;
     std::stable_sort(lps.begin(), lps.end(),
                      [&](int a, int b) { return items[a].work > items[b].work; });
-    // split only if the combined (max m, max ldw) layout would overflow
-    std::vector<ClassPlan> parts;
-    std::vector<std::vector<int>> members;
+    ClassPlan c;
+    c.K = kv.first < 100 ? 1 : kv.first - 100;
+    int nl = 1;
     for (int lp : lps) {
-      bool placed = false;
-      for (size_t ci = 0; ci < parts.size() && !placed; ++ci) {
-        ClassPlan& c = parts[ci];
-        const int mm = std::max(c.max_m, p->m[lp]);
-        const int ll = std::max(c.max_ldw, items[lp].ldw);
-        const int vv = std::max(c.max_nv, items[lp].nv);
-        const int lim =
-            std::max(budget, Layout(p->m[lp], items[lp].ldw, items[lp].nv, elem, se).total);
-        if (Layout(mm, ll, vv, elem, se).total <= std::min(lim, max_smem)) {
-          c.max_m = mm;
-          c.max_ldw = ll;
-          c.max_nv = vv;
-          c.max_na = std::max(c.max_na, p->na[lp]);
-          c.work += items[lp].work;
-          c.nt = std::max(c.nt, items[lp].nl);
-          members[ci].push_back(lp);
-          placed = true;
-        }
-      }
-      if (!placed) {
-        ClassPlan c;
-        c.K = kv.first;
-        c.max_m = p->m[lp];
-        c.max_ldw = items[lp].ldw;
-        c.max_nv = items[lp].nv;
-        c.max_na = p->na[lp];
-        c.work = items[lp].work;
-        c.nt = items[lp].nl;
-        parts.push_back(c);
-        members.push_back({lp});
-      }
+      c.smem = std::max(c.smem, items[lp].bytes);
+      c.max_m = std::max(c.max_m, p->m[lp]);
+      c.max_na = std::max(c.max_na, p->na[lp]);
+      c.work += items[lp].work;
+      nl = std::max(nl, items[lp].nl);
     }
-    for (size_t ci = 0; ci < parts.size(); ++ci) {
-      ClassPlan c = parts[ci];
-      c.smem = Layout(c.max_m, c.max_ldw, c.max_nv, elem, se).total;
-      // threads: every member's row of vector lanes at least once (c.nt
-      // holds the widest member's lane count here)
-      c.nt = pick_threads(p, c.nt, c.smem, kernel_regs<T>(c.K > 1), c.K,
-                          p->opt.threads_per_cta, &c.ctas_per_sm);
-      c.count = (int)members[ci].size();
-      c.order_off = (int)p->order.size();
-      p->order.insert(p->order.end(), members[ci].begin(), members[ci].end());
-      int per_sm = 0, clusters = 0;
-      int rc = occupancy<T>(c, &per_sm, &clusters);
-      if (rc) return rc;
-      int slots = c.K == 1 ? per_sm * p->sm_count : clusters;
-      if (c.K == 1) c.ctas_per_sm = per_sm;
-      if (slots <= 0)
-        return fail(BLPG_ETOOBIG, "class K=%d nt=%d smem=%d cannot be resident", c.K,
-                    c.nt, c.smem);
-      // share of the GPU proportional to the class's work (classes co-run)
-      const double share = total_work > 0 ? c.work / total_work : 1.0;
-      int want = (int)std::ceil(share * slots);
-      want = std::max(1, std::min(want, slots));
-      c.grid = std::min(want, c.count) * c.K;
-      p->classes.push_back(c);
-    }
+    // threads: every member's row of vector lanes at least once
+    c.nt = pick_threads(p, nl, c.smem, kernel_regs<T>(c.K > 1), c.K, p->opt.threads_per_cta,
+                        &c.ctas_per_sm);
+    c.count = (int)lps.size();
+    int per_sm = 0, clusters = 0;
+    int rc = occupancy<T>(c, &per_sm, &clusters);
+    if (rc) return rc;
+    const int slots = c.K == 1 ? per_sm * p->sm_count : clusters;
+    if (slots <= 0)
+      return fail(BLPG_ETOOBIG, "class K=%d nt=%d smem=%d cannot be resident", c.K, c.nt,
+                  c.smem);
+    if (c.K == 1) c.ctas_per_sm = per_sm;
+    c.grid = std::min(slots, c.count) * c.K;  // full residency (persistent CTAs)
+    built.emplace_back(c, lps);
   }
-  std::stable_sort(p->classes.begin(), p->classes.end(),
-                   [](const ClassPlan& a, const ClassPlan& b) { return a.work > b.work; });
+  // heaviest LPs first: clusters by size, then single-CTA classes by layout
+  std::stable_sort(built.begin(), built.end(), [](const auto& a, const auto& b) {
+    if (a.first.K != b.first.K) return a.first.K > b.first.K;
+    return a.first.smem > b.first.smem;
+  });
+  for (auto& cb : built) {
+    ClassPlan c = cb.first;
+    c.order_off = (int)p->order.size();
+    p->order.insert(p->order.end(), cb.second.begin(), cb.second.end());
+    p->classes.push_back(c);
+  }
   return BLPG_OK;
 }
 
@@ -350,11 +332,9 @@ static int launch_one(blpg_plan* p, size_t ci, const LpArgs& args, cudaStream_t 
   ca.count = c.count;
   ca.ticket = p->d_tickets + ci;
   ca.K = c.K;
-  ca.max_m = c.max_m;
-  ca.max_ldw = c.max_ldw;
   ca.max_na = c.max_na;
-  ca.max_nv = c.max_nv;
   ca.se = p->opt.pricing == BLPG_PRICE_STEEPEST ? 1 : 0;
+  ca.smem = c.smem;
   if (c.K == 1) {
     dev::solve_kernel<T, false><<<c.grid, c.nt, c.smem, s>>>(args, ca);
     CK(cudaGetLastError());

@@ -75,13 +75,12 @@ int32_t run(int32_t count, int32_t max_m, int32_t max_n, const blpg::dev::LpArgs
   using namespace blpg::dev;
   constexpr int V = VecT<T>::V;
   const int max_smem = (int)prop.sharedMemPerBlockOptin;
-  int K = 0, nt = 0, smem = 0, ldw = 0;
+  int K = 0, nt = 0, smem = 0;
   for (int k = 1; k <= 8; k *= 2) {
     Geom g(max_m, max_n, 0, k, V);
     Layout L(max_m, g.ldw, max_n + max_m, (int)sizeof(T));
     if (L.total <= max_smem && g.nl <= 512) {
       K = k;
-      ldw = g.ldw;
       smem = L.total;
       int G = g.nl >= 256 ? 1 : 256 / g.nl;
       nt = round_up(G * g.nl, 32);
@@ -97,11 +96,9 @@ int32_t run(int32_t count, int32_t max_m, int32_t max_n, const blpg::dev::LpArgs
   ca.count = count;
   ca.ticket = scratch;
   ca.K = K;
-  ca.max_m = max_m;
-  ca.max_ldw = ldw;
   ca.max_na = 0;
-  ca.max_nv = max_n + max_m;
   ca.se = 0;  // Dantzig pricing: no column norms
+  ca.smem = smem;
   noalloc_reset<<<(count + 255) / 256 > 0 ? (count + 255) / 256 : 1, 256, 0, s>>>(scratch, count);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)

@@ -98,11 +98,9 @@ struct ClassArgs {
   int32_t count;
   int32_t* ticket;  // queue head, zeroed before the launch
   int32_t K;        // CTAs per LP (cluster size)
-  int32_t max_m;    // smem layout is sized for these
-  int32_t max_ldw;
-  int32_t max_na;   // artificial columns (two-phase LPs)
-  int32_t max_nv;   // variables n + m + na
+  int32_t max_na;   // artificial columns (two-phase LPs); LPs with more are refused
   int32_t se;       // steepest-edge pricing: the layout holds column norms
+  int32_t smem;     // dynamic shared memory per CTA; LPs whose layout is larger are refused
 };
 
 template <typename T>
@@ -139,14 +137,22 @@ struct Geom {
   }
 };
 
-// Shared-memory layout of a class (bytes).  Identical on host and device.
+// Shared-memory layout of one LP (bytes), identical on host and device.  A
+// fixed header (the CTA's state and argmin scratch) comes first; the LP's
+// regions follow, sized for its own m, column width ldw and variable count
+// nv, so a CTA lays out each LP it takes within its allocation and a class
+// only needs the largest member's total.
 struct Layout {
   int tab, colA, colB, rhsx, basis, flags, cvar, vpos, ext, red, state, gam, total;
-  __host__ __device__ Layout(int max_m, int max_ldw, int max_nv, int elem, int se = 0) {
-    int mp1 = round_up(max_m + 1, 4);
-    int nvp = round_up(max_nv, 4);
-    tab = 0;
-    int off = round_up((max_m + 1) * max_ldw * elem, 16);
+  __host__ __device__ Layout(int m, int ldw, int nv, int elem, int se = 0) {
+    const int mp1 = round_up(m + 1, 4);
+    const int nvp = round_up(nv, 4);
+    state = 0;
+    int off = 224;
+    red = off;
+    off += 3 * 32 * 16;  // three argmin scratch buffers (pricing, ratio, Harris)
+    tab = off;
+    off += round_up((m + 1) * ldw * elem, 16);
     colA = off;
     off += round_up(mp1 * elem, 16);
     colB = off;
@@ -170,18 +176,14 @@ struct Layout {
     // recomputed after every refresh)
     gam = -1;
     if (se) {
-      if (ext_bytes >= max_ldw * 8) {
+      if (ext_bytes >= ldw * 8) {
         gam = ext;
       } else {
         off = round_up(off, 16);
         gam = off;
-        off += round_up(max_ldw * 8, 16);
+        off += round_up(ldw * 8, 16);
       }
     }
-    red = off;
-    off += 3 * 32 * 16;  // three argmin scratch buffers (pricing, ratio, Harris)
-    state = off;
-    off += 224;
     total = off;
   }
 };
@@ -1465,6 +1467,22 @@ struct Solver {
     __syncthreads();
   }
 
+  // Per-LP regions of the shared-memory layout.
+  __device__ void place(const Layout& L, int m) {
+    tab = reinterpret_cast<T*>(smem + L.tab);
+    col0 = reinterpret_cast<T*>(smem + L.colA);
+    col1 = reinterpret_cast<T*>(smem + L.colB);
+    rhsx = reinterpret_cast<T*>(smem + L.rhsx);
+    basis = reinterpret_cast<int*>(smem + L.basis);
+    flags = reinterpret_cast<int*>(smem + L.flags);
+    cvar = reinterpret_cast<int*>(smem + L.cvar);
+    vpos = reinterpret_cast<int*>(smem + L.vpos);
+    xr = reinterpret_cast<double*>(smem + L.ext);
+    yr = xr + round_up(m + 1, 4);
+    rf = reinterpret_cast<float*>(yr + round_up(m + 1, 4));
+    gam = L.gam >= 0 ? reinterpret_cast<unsigned long long*>(smem + L.gam) : nullptr;
+  }
+
   __device__ void run(const LpArgs& a, const ClassArgs& ca) {
     const int tid = threadIdx.x, nt = blockDim.x;
     constexpr bool kFP32 = sizeof(T) == 4;
@@ -1488,7 +1506,8 @@ struct Solver {
       for (int i = tid; i < m; i += nt) na += b[i] < 0.0 ? 1 : 0;
       na = block_sum(na);
       const Geom g(m, n, na, K, V);
-      if (m > ca.max_m || g.ldw > ca.max_ldw || na > ca.max_na || n + m + na > ca.max_nv) {
+      const Layout L(m, g.ldw, n + m + na, (int)sizeof(T), ca.se);
+      if (L.total > ca.smem || na > ca.max_na || g.nl > (int)blockDim.x) {
         // the LP does not fit the layout this plan was built for (e.g. a
         // plan made without b has no room for phase-I columns): refuse it
         if (rank == 0 && tid == 0) {
@@ -1500,6 +1519,7 @@ struct Solver {
         __syncthreads();
         continue;
       }
+      place(L, m);
       const int c0 = rank * g.cw;
       const int lc = max(0, min(g.cw, g.Wc - c0));
       load(g, c0, lc, A, b, c);
@@ -1646,20 +1666,8 @@ template <typename T, bool CLUSTER>
 __global__ void __launch_bounds__(512, 1) solve_kernel(const LpArgs a, const ClassArgs ca) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Solver<T, CLUSTER> s;
-  const Layout L(ca.max_m, ca.max_ldw, ca.max_nv, (int)sizeof(T), ca.se);
+  const Layout L(0, 0, 0, (int)sizeof(T), ca.se);  // the fixed header
   s.smem = smem_raw;
-  s.tab = reinterpret_cast<T*>(smem_raw + L.tab);
-  s.col0 = reinterpret_cast<T*>(smem_raw + L.colA);
-  s.col1 = reinterpret_cast<T*>(smem_raw + L.colB);
-  s.rhsx = reinterpret_cast<T*>(smem_raw + L.rhsx);
-  s.basis = reinterpret_cast<int*>(smem_raw + L.basis);
-  s.flags = reinterpret_cast<int*>(smem_raw + L.flags);
-  s.cvar = reinterpret_cast<int*>(smem_raw + L.cvar);
-  s.vpos = reinterpret_cast<int*>(smem_raw + L.vpos);
-  s.xr = reinterpret_cast<double*>(smem_raw + L.ext);
-  s.yr = s.xr + round_up(ca.max_m + 1, 4);
-  s.rf = reinterpret_cast<float*>(s.yr + round_up(ca.max_m + 1, 4));
-  s.gam = L.gam >= 0 ? reinterpret_cast<unsigned long long*>(smem_raw + L.gam) : nullptr;
   s.redP = reinterpret_cast<Key*>(smem_raw + L.red);
   s.redR = s.redP + 32;
   s.redH = s.redP + 64;
