@@ -166,12 +166,17 @@ typedef struct blpg_result {
 /* Bits of blpg_result.info. */
 enum {
   BLPG_INFO_WARM = 1,     /* a basis hint was used */
-  BLPG_INFO_FALLBACK = 2, /* hinted basis primal- and dual-infeasible: cold solve */
+  BLPG_INFO_FALLBACK = 2, /* cold solve after a hint: the hinted basis was primal- and
+                             dual-infeasible, or (FP32) the warm-started solve ended on
+                             a basis the FP64 refresh could not verify */
   BLPG_INFO_PARTIAL = 4,  /* some hinted columns found no pivot (singular) */
   BLPG_INFO_DUAL = 8,     /* dual simplex pivots were taken */
   BLPG_INFO_REFRESH = 16, /* FP64 refresh of the FP32 tableau ran */
   BLPG_INFO_REPAIR = 32,  /* an FP64 check found a violation: more pivots */
-  BLPG_INFO_SHIFT = 64    /* hinted basis infeasible both ways: cost-shifted dual phase */
+  BLPG_INFO_SHIFT = 64,   /* hinted basis infeasible both ways: cost-shifted dual phase */
+  BLPG_INFO_UNVERIFIED = 128 /* FP32: the FP64 refresh did not converge on the final
+                                basis (the FP32 tableau is too inaccurate to check it);
+                                the status is BLPG_UNDEF */
 };
 
 /* Fill *opt with the defaults above. */

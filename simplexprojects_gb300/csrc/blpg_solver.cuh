@@ -92,6 +92,7 @@ constexpr int kInfoDual = 8;       // dual simplex pivots were taken
 constexpr int kInfoRefresh = 16;   // FP64 refresh of the FP32 tableau ran
 constexpr int kInfoRepair = 32;    // a refresh found a violation (more pivots)
 constexpr int kInfoShift = 64;     // hinted basis infeasible both ways: cost-shifted dual phase
+constexpr int kInfoUnverified = 128;  // FP32: the FP64 refresh could not verify the final basis
 
 struct ClassArgs {
   const int32_t* order;  // LP ids of this class, heaviest first
@@ -342,6 +343,11 @@ __device__ __forceinline__ double norm_value(unsigned long long u) {
 // Status codes (GLPK numbering, as blpg.h)
 constexpr int kUndef = 1, kNoFeas = 4, kOpt = 5, kUnbnd = 6;
 constexpr int kRefresh = 100;  // internal: the primal loop paused for a refresh
+constexpr int kUnverified = 101;  // internal: the FP64 refresh could not verify the basis
+// Iterative-refinement steps of the FP64 refresh; a refresh whose last
+// correction is still above 1e-10 of the values reports no convergence (the
+// FP32 B^-1 is too inaccurate to verify the basis).
+constexpr int kRefineIters = 4;
 
 struct SharedState {
   int ticket;
@@ -1087,7 +1093,8 @@ struct Solver {
   // split.  All work is proportional to ns, the number of structural basics
   // (= the number of nonbasic slacks), except the reduced costs, one FP64
   // dot product per nonbasic structural column.  Returns bit 0: x_B >= -ptol,
-  // bit 1: d >= -opt_tol (both judged in FP64).  Single-phase LPs only.
+  // bit 1: d >= -opt_tol (both judged in FP64), bit 2: both refinements
+  // converged (without it bits 0 and 1 prove nothing).  Single-phase LPs only.
   __device__ int refresh(const Geom& g, const double* A, const double* b, const double* c,
                          const LpArgs& a) {
     const int m = g.m, n = g.n;
@@ -1144,7 +1151,8 @@ struct Solver {
       // floats order like their bit patterns, so a shared atomicMax works.
       unsigned* mx = &sh->aux.w2;  // [0] max |correction|, [1] max |value|
       for (int i = tid; i < m; i += nt) xr[i] = (double)tab[(size_t)i * g.ldw + g.cw];
-      for (int it = 0; it < 2; ++it) {
+      bool xconv = false;
+      for (int it = 0; it < kRefineIters; ++it) {
         if (tid == 0) mx[0] = mx[1] = 0u;
         __syncthreads();
         // r_k = b_k - sum_t A_k,col_t x_t - x_(slack k, when basic): one
@@ -1202,7 +1210,10 @@ struct Solver {
           }
         }
         __syncthreads();
-        if (__uint_as_float(mx[0]) <= 1e-10f * fmaxf(1.f, __uint_as_float(mx[1]))) break;
+        if (__uint_as_float(mx[0]) <= 1e-10f * fmaxf(1.f, __uint_as_float(mx[1]))) {
+          xconv = true;
+          break;
+        }
         __syncthreads();
       }
       __syncthreads();
@@ -1216,7 +1227,8 @@ struct Solver {
       // order; P = 1 above 96 basics
       const int P = (ns > 0 && ns <= 96) ? min(4, 192 / ns) : 1;
       const int kc = ceil_div(m, P);
-      for (int it = 0; it < 2; ++it) {
+      bool yconv = false;
+      for (int it = 0; it < kRefineIters; ++it) {
         if (tid == 0) mx[0] = mx[1] = 0u;
         __syncthreads();
         // s_i = cB_i - (B^T y)_i: structural basic in row i with column col:
@@ -1288,7 +1300,10 @@ struct Solver {
           }
         }
         __syncthreads();
-        if (__uint_as_float(mx[0]) <= 1e-10f * fmaxf(1.f, __uint_as_float(mx[1]))) break;
+        if (__uint_as_float(mx[0]) <= 1e-10f * fmaxf(1.f, __uint_as_float(mx[1]))) {
+          yconv = true;
+          break;
+        }
         __syncthreads();
       }
       // Reduced costs d_j = y^T a_j - c_j of the nonbasic structural
@@ -1340,7 +1355,7 @@ struct Solver {
       }
       badd = __syncthreads_or(badd ? 1 : 0) != 0;
       badp = __syncthreads_or(badp ? 1 : 0) != 0;
-      ok = (badp ? 0 : 1) | (badd ? 0 : 2);
+      ok = (badp ? 0 : 1) | (badd ? 0 : 2) | (xconv && yconv ? 4 : 0);
       if (tid == 0) sh->aux.w1 = (unsigned)ok;
     }
     if (CLUSTER) {
@@ -1548,78 +1563,110 @@ struct Solver {
           st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
         }
       } else {
-        st = -1;
-        if (a.hint) {
-          info |= kInfoWarm;
-          if (crash(g, c0, a.hint + a.offbasis[lp], a, pivots, cur, lc) > 0) info |= kInfoPartial;
-          // feasibility of the crashed basis judged on the tableau itself
-          // (the final FP64 refresh verifies whatever basis the finish ends on)
-          const int fl = check_feasible(g, c0, lc, ptol, opt_tol);
-          if (fl & 1) {
-            st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
-          } else if (fl & 2) {
-            info |= kInfoDual;
-            st = dual_loop(g, c0, lc, a, max_piv, pivots, cur, ptol);
-            if (st == kOpt) st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
-          } else if (a.warm_mode == 1) {
-            // infeasible both ways: shift the costs of the columns with
-            // d_j < -opt_tol to small distinct positive values (dual
-            // feasible), dual simplex to a primal-feasible basis, restore the
-            // true costs, primal simplex
-            info |= kInfoDual | kInfoShift;
-            T* drow = tab + (size_t)m * g.ldw;
-            for (int lj = tid; lj < lc; lj += nt) {
-              const int j = cvar[c0 + lj];
-              if (j < n + m && drow[lj] < -opt_tol)
-                drow[lj] = (T)a.shift * (T(1) + (T)((j * 7919) % 1000) / T(1000));
-            }
-            __syncthreads();
-            st = dual_loop(g, c0, lc, a, max_piv, pivots, cur, ptol);
-            if (st == kOpt) {
-              objective_row(g, c0, lc, c, false);
-              __syncthreads();
-              st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
-            }
-          }
-          if (st < 0 || st == kNoFeas) {
-            // infeasible both ways (or dual simplex stuck): cold solve
+        // FP32: a solve whose final basis the FP64 refresh cannot verify is
+        // repeated cold from the slack basis when it was warm-started, with
+        // a pivot budget of its own; a cold one is reported BLPG_UNDEF.
+        int budget = max_piv;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+          st = -1;
+          const bool warm = attempt == 0 && a.hint;
+          if (attempt > 0) {
             info |= kInfoFallback;
             if (CLUSTER) csync();
             load(g, c0, lc, A, b, c);
             refreshed = false;
             bland = false;
             degen = 0;
-            st = -1;
+            budget = pivots + max_piv;
           }
-        }
-        if (st < 0) {
-          const int period = kFP32 ? a.refresh_period : 0;
-          for (;;) {
-            st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur, period);
-            if (st != kRefresh) break;
-            if (CLUSTER) csync();
-            refresh(g, A, b, c, a);
-            refreshed = true;
-            info |= kInfoRefresh;
-          }
-        }
-        // FP32: verify the final basis in FP64 and repair if needed
-        if (kFP32 && st == kOpt) {
-          for (int round = 0; round < 4; ++round) {
-            if (CLUSTER) csync();
-            const int fl = refresh(g, A, b, c, a);
-            refreshed = true;
-            info |= kInfoRefresh;
-            if ((fl & 3) == 3) break;
-            info |= kInfoRepair;
-            if (!(fl & 1)) {
+          if (warm) {
+            info |= kInfoWarm;
+            if (crash(g, c0, a.hint + a.offbasis[lp], a, pivots, cur, lc) > 0)
+              info |= kInfoPartial;
+            // feasibility of the crashed basis judged on the tableau itself
+            // (the final FP64 refresh verifies whatever basis the finish ends on)
+            const int fl = check_feasible(g, c0, lc, ptol, opt_tol);
+            if (fl & 1) {
+              st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
+            } else if (fl & 2) {
               info |= kInfoDual;
-              st = dual_loop(g, c0, lc, a, max_piv, pivots, cur, ptol);
+              st = dual_loop(g, c0, lc, a, budget, pivots, cur, ptol);
+              if (st == kOpt) st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
+            } else if (a.warm_mode == 1) {
+              // infeasible both ways: shift the costs of the columns with
+              // d_j < -opt_tol to small distinct positive values (dual
+              // feasible), dual simplex to a primal-feasible basis, restore
+              // the true costs, primal simplex
+              info |= kInfoDual | kInfoShift;
+              T* drow = tab + (size_t)m * g.ldw;
+              for (int lj = tid; lj < lc; lj += nt) {
+                const int j = cvar[c0 + lj];
+                if (j < n + m && drow[lj] < -opt_tol)
+                  drow[lj] = (T)a.shift * (T(1) + (T)((j * 7919) % 1000) / T(1000));
+              }
+              __syncthreads();
+              st = dual_loop(g, c0, lc, a, budget, pivots, cur, ptol);
+              if (st == kOpt) {
+                objective_row(g, c0, lc, c, false);
+                __syncthreads();
+                st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
+              }
+            }
+            if (st < 0 || st == kNoFeas) {
+              // infeasible both ways (or dual simplex stuck): cold solve
+              info |= kInfoFallback;
+              if (CLUSTER) csync();
+              load(g, c0, lc, A, b, c);
+              refreshed = false;
+              bland = false;
+              degen = 0;
+              st = -1;
+            }
+          }
+          if (st < 0) {
+            const int period = kFP32 ? a.refresh_period : 0;
+            for (;;) {
+              st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur, period);
+              if (st != kRefresh) break;
+              if (CLUSTER) csync();
+              refresh(g, A, b, c, a);
+              refreshed = true;
+              info |= kInfoRefresh;
+            }
+          }
+          // FP32: verify the final basis in FP64 and repair if needed (at
+          // most four repairs, each verified by another refresh)
+          if (kFP32 && st == kOpt) {
+            bool verified = false;
+            for (int round = 0; round <= 4; ++round) {
+              if (CLUSTER) csync();
+              const int fl = refresh(g, A, b, c, a);
+              refreshed = true;
+              info |= kInfoRefresh;
+              if (!(fl & 4)) break;  // refinement did not converge
+              if ((fl & 3) == 3) {
+                verified = true;
+                break;
+              }
+              if (round == 4) break;
+              info |= kInfoRepair;
+              if (!(fl & 1)) {
+                info |= kInfoDual;
+                st = dual_loop(g, c0, lc, a, budget, pivots, cur, ptol);
+                if (st != kOpt) break;
+              }
+              st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
               if (st != kOpt) break;
             }
-            st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
-            if (st != kOpt) break;
+            if (st == kOpt && !verified) st = kUnverified;
           }
+          // a warm start that ends unverified or at the pivot cap: once more, cold
+          if (kFP32 && warm && (st == kUnverified || st == kUndef)) continue;
+          break;
+        }
+        if (st == kUnverified) {
+          st = kUndef;
+          info |= kInfoUnverified;
         }
       }
       if (CLUSTER) csync();

@@ -153,3 +153,19 @@ def test_warm_start_checkpoint_roundtrip(built, tmp_path):
     d = ws.device_inputs(train)
     import torch
     assert torch.equal(ws.features(d), ws2.features(d))
+
+
+@pytest.mark.parametrize("pricing", ["dantzig", "steepest"])
+def test_fp32_warm_start_is_verified(built, pricing):
+    """FP32 warm starts on the uneven workload (unbounded columns, zero-b
+    rows): crash and dual simplex in FP32 can end on a tableau too inaccurate
+    to trust.  The FP64 refresh must then fail to converge, and the LP is
+    re-solved cold: every optimal objective within 1e-6, statuses as FP64."""
+    batch = sp.generate(1, 2048, seed=sp.DEFAULT_SEED)
+    exact = ref.solve_batch(batch, "fp64", want_basis=True)
+    g = sp.solve(batch, "fp32", pricing=pricing, hint=exact.basis)
+    assert np.array_equal(g.status, exact.status)
+    opt = exact.status == 5
+    rel = np.abs(g.objective[opt] - exact.objective[opt]) / np.maximum(np.abs(exact.objective[opt]), 1.0)
+    assert rel.max() <= 1e-6
+    assert ((g.info & 128) == 0).all()  # nothing left unverified
