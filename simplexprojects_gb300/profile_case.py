@@ -6,9 +6,12 @@ the solve twice (one warm-up, one capture target), then prints the class plan,
 the status histogram and the pivot total. It holds a few MB on the device, so
 a full-metric capture of one solve_kernel launch ends within a minute:
 
-    python -m simplexprojects_gb300.profile_case 3 152 fp32
+    python -m simplexprojects_gb300.profile_case 3 304 fp32 steepest
     ncu --set full --clock-control none -k regex:solve_kernel -s 1 -c 1 \
-        -o prof python -m simplexprojects_gb300.profile_case 3 152 fp32
+        -o prof python -m simplexprojects_gb300.profile_case 3 304 fp32 steepest
+
+Arguments: workload kind, LP count, precision (fp64 | fp32), pricing
+(dantzig | steepest; default dantzig).
 """
 from __future__ import annotations
 
@@ -22,10 +25,11 @@ def main(argv=None):
     kind = int(argv[0]) if len(argv) > 0 else 1
     count = int(argv[1]) if len(argv) > 1 else 1500
     prec = argv[2] if len(argv) > 2 else "fp64"
+    pricing = argv[3] if len(argv) > 3 else "dantzig"
     from .lp import DEFAULT_SEED, generate
     from .solver import DeviceBatch
     batch = generate(kind, count, seed=DEFAULT_SEED, share_family_A=True)
-    db = DeviceBatch(batch, prec)
+    db = DeviceBatch(batch, prec, pricing=pricing)
     for _ in range(2):
         db.run()
     r = db.result()
