@@ -593,11 +593,31 @@ struct Solver {
     const int sl = local_slot(s, c0, cw);
     const bool has_s = sl >= lane * V && sl < lane * V + V;
     const int se = sl - lane * V;
-    // kU rows per step, every load issued before any store (rows grp,
-    // grp + G, ... are disjoint, so this only adds parallelism).  Row r
-    // already holds the divided pivot row and is only read.
-    constexpr int kU = 2;
+    // Elements of the entering slot, taken as 0 before the elimination.
+    bool zs[V];
+#pragma unroll
+    for (int e = 0; e < V; ++e) zs[e] = has_s && se == e;
     VT sq = VT{};  // steepest edge: sum of squares of this lane's final values
+    // One row: the elimination is computed unconditionally and stored only
+    // where it applies (a zero multiplier leaves the row as it is; row r
+    // already holds the divided pivot row), so the body has no divergent
+    // branch, only predicated stores.
+    auto row = [&](const int i, const T f, const VT t) {
+      const bool upd = f != T(0) && i != r;
+      VT tz = t;
+#pragma unroll
+      for (int e = 0; e < V; ++e)
+        if (zs[e]) vset(tz, e, T(0));
+      const VT tn = v_fma(f, p, tz);
+      if (upd) *reinterpret_cast<VT*>(tb + (size_t)i * ldw + lane * V) = tn;
+      const VT tf = upd ? tn : t;
+      if (has_q) colx_next[i] = vget<VT, T>(tf, qe);
+      if (has_rhs) rhsx[i] = vget<VT, T>(tf, 0);
+      if (SE) sq = v_sq(tf, sq);
+    };
+    // kU rows per step, every load issued before any store (rows grp,
+    // grp + G, ... are disjoint, so this only adds parallelism)
+    constexpr int kU = 4;
     int i0 = grp;
     for (; i0 + (kU - 1) * G < m; i0 += kU * G) {
       T f[kU];
@@ -609,33 +629,16 @@ struct Solver {
         t[u] = *reinterpret_cast<const VT*>(tb + (size_t)i * ldw + lane * V);
       }
 #pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        const int i = i0 + u * G;
-        if (f[u] != T(0) && i != r) {  // a zero multiplier leaves the row as it is
-          if (has_s) vset(t[u], se, T(0));
-          t[u] = v_fma(f[u], p, t[u]);
-          *reinterpret_cast<VT*>(tb + (size_t)i * ldw + lane * V) = t[u];
-        }
-        if (has_q) colx_next[i] = vget<VT, T>(t[u], qe);
-        if (has_rhs) rhsx[i] = vget<VT, T>(t[u], 0);
-        if (SE) sq = v_sq(t[u], sq);
-      }
+      for (int u = 0; u < kU; ++u) row(i0 + u * G, f[u], t[u]);
     }
-    for (; i0 < m; i0 += G) {
-      const T f = pcol[i0];
-      VT t = *reinterpret_cast<const VT*>(tb + (size_t)i0 * ldw + lane * V);
-      if (f != T(0) && i0 != r) {
-        if (has_s) vset(t, se, T(0));
-        t = v_fma(f, p, t);
-        *reinterpret_cast<VT*>(tb + (size_t)i0 * ldw + lane * V) = t;
-      }
-      if (has_q) colx_next[i0] = vget<VT, T>(t, qe);
-      if (has_rhs) rhsx[i0] = vget<VT, T>(t, 0);
-      if (SE) sq = v_sq(t, sq);
-    }
+    for (; i0 < m; i0 += G)
+      row(i0, pcol[i0], *reinterpret_cast<const VT*>(tb + (size_t)i0 * ldw + lane * V));
     if (SE) {
+      // columns visited in a rotated order, so that the 64-bit counters of
+      // one instruction fall in distinct banks (two wavefronts, not eight)
 #pragma unroll
-      for (int e = 0; e < V; ++e) {
+      for (int e2 = 0; e2 < V; ++e2) {
+        const int e = (e2 + (lane >> 2)) & (V - 1);
         const int lj = lane * V + e;
         if (lj < lc) atomicAdd(&gam[lj], norm_fixed(vget<VT, T>(sq, e)));
       }
