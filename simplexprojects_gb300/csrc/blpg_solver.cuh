@@ -206,13 +206,16 @@ __device__ __forceinline__ bool key_less(const Key& a, const Key& b) {
   return a.w2 < b.w2;
 }
 
+// W1 = false: every real key has w1 == 0 (FP32 values fit w0), so that word
+// is not reduced (an all-empty warp then returns w1 = 0, still empty by w2).
+template <bool W1 = true>
 __device__ __forceinline__ Key warp_min(const Key& k) {
   const unsigned full = 0xffffffffu;
   Key r;
   r.w0 = __reduce_min_sync(full, k.w0);
   bool e0 = k.w0 == r.w0;
-  r.w1 = __reduce_min_sync(full, e0 ? k.w1 : ~0u);
-  bool e1 = e0 && k.w1 == r.w1;
+  r.w1 = W1 ? __reduce_min_sync(full, e0 ? k.w1 : ~0u) : 0u;
+  bool e1 = e0 && (!W1 || k.w1 == r.w1);
   r.w2 = __reduce_min_sync(full, e1 ? k.w2 : ~0u);
   bool e2 = e1 && k.w2 == r.w2;
   r.w3 = __reduce_min_sync(full, e2 ? k.w3 : ~0u);
@@ -221,14 +224,15 @@ __device__ __forceinline__ Key warp_min(const Key& k) {
 
 // Block-wide argmin: every thread returns the winner.  Contains exactly one
 // __syncthreads; `red` (32 keys) must not be reused before another barrier.
+template <bool W1 = true>
 __device__ __forceinline__ Key block_min(const Key& k, Key* red) {
-  Key w = warp_min(k);
+  Key w = warp_min<W1>(k);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) red[warp] = w;
   __syncthreads();
   const int nw = (int)(blockDim.x >> 5);
   Key v = lane < nw ? red[lane] : key_none();
-  return warp_min(v);
+  return warp_min<W1>(v);
 }
 
 // Pricing key of reduced cost d of variable j in column slot s (only
@@ -369,6 +373,7 @@ template <typename T, bool CLUSTER>
 struct Solver {
   using VT = typename VecT<T>::type;
   static constexpr int V = VecT<T>::V;
+  static constexpr bool kW1 = sizeof(T) == 8;  // keys use w1 only for FP64 values
 
   unsigned char* smem;
   T* tab;
@@ -432,7 +437,7 @@ struct Solver {
         if (key_less(kk, k)) k = kk;
       }
     }
-    k = block_min(k, redP);
+    k = block_min<kW1>(k, redP);
     return cluster_min(k);
   }
 
@@ -452,34 +457,49 @@ struct Solver {
   // relaxed by feas_tol, pass 2 takes the largest pivot entry among rows
   // within the bound (ties by lowest basic variable).  The oracle's ratio()
   // performs the same operations.
-  __device__ Key ratio(const Geom& g, const T* colx, T piv_tol, T feas_tol, bool harris,
-                       T& theta) {
+  // With fuse_sl >= 0 the entering column (local slot fuse_sl) and the RHS
+  // are read from the tableau and copied into colx / rhsx on the way, the
+  // first pass's barrier publishing them (single-CTA steepest-edge loop).
+  __device__ Key ratio(const Geom& g, T* colx, T piv_tol, T feas_tol, bool harris, T& theta,
+                       int fuse_sl = -1) {
+    auto fetch = [&](int i, T& a, T& rh) {
+      if (fuse_sl >= 0) {
+        a = tab[(size_t)i * g.ldw + fuse_sl];
+        rh = tab[(size_t)i * g.ldw + g.cw];
+        colx[i] = a;
+        rhsx[i] = rh;
+      } else {
+        a = colx[i];
+        rh = rhsx[i];
+      }
+    };
+    if (fuse_sl >= 0 && threadIdx.x == 0) colx[g.m] = tab[(size_t)g.m * g.ldw + fuse_sl];
     Key k = key_none();
     if (!harris) {
       for (int i = threadIdx.x; i < g.m; i += blockDim.x) {
-        const T a = colx[i];
+        T a, rh;
+        fetch(i, a, rh);
         if (a > piv_tol) {
-          const T rh = rhsx[i];
           const T th = rh > T(0) ? rh / a : T(0);
           Key kk = ratio_key(th, basis[i], i);
           if (key_less(kk, k)) k = kk;
         }
       }
-      k = block_min(k, redR);
+      k = block_min<kW1>(k, redR);
       theta = key_theta(k, T(0));
       return k;
     }
     for (int i = threadIdx.x; i < g.m; i += blockDim.x) {
-      const T a = colx[i];
+      T a, rh;
+      fetch(i, a, rh);
       if (a > piv_tol) {
-        const T rh = rhsx[i];
         const T rr = rh > T(0) ? rh : T(0);
         const T th1 = (rr + feas_tol) / a;
         Key kk = ratio_key(th1, 0, i);
         if (key_less(kk, k)) k = kk;
       }
     }
-    k = block_min(k, redR);
+    k = block_min<kW1>(k, redR);
     if (k.w2 == ~0u) return k;
     const T tmax = key_theta(k, T(0));
     Key k2 = key_none();
@@ -494,7 +514,7 @@ struct Solver {
         }
       }
     }
-    k2 = block_min(k2, redH);
+    k2 = block_min<kW1>(k2, redH);
     const int r = (int)k2.w3;
     const T a = colx[r], rh = rhsx[r];
     theta = rh > T(0) ? rh / a : T(0);
@@ -514,33 +534,31 @@ struct Solver {
     T* prow = tab + (size_t)r * g.ldw;
     T* drow = tab + (size_t)g.m * g.ldw;
     const int sl = local_slot(s, c0, g.cw);
+    const bool price = price_cols > 0;
     Key k = key_none();
-    for (int v = threadIdx.x; v < g.nl; v += blockDim.x) {
-      const bool has_s = sl >= v * V && sl < v * V + V;
-      VT p = *reinterpret_cast<const VT*>(prow + v * V);
-      p = v_div(p, piv);
-      if (has_s) vset(p, sl - v * V, rcp);
-      *reinterpret_cast<VT*>(prow + v * V) = p;
-      VT d = *reinterpret_cast<const VT*>(drow + v * V);
+    // one element per thread (the row is short: a few hundred entries), so
+    // that each thread waits on one division, not a vector of them
+    for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) {
+      const T p = lj == sl ? rcp : sdiv(prow[lj], piv);
+      prow[lj] = p;
+      T d = drow[lj];
       if (dq != T(0)) {
-        if (has_s) vset(d, sl - v * V, T(0));
-        d = v_fma(dq, p, d);
-        *reinterpret_cast<VT*>(drow + v * V) = d;
+        d = fma_t(-dq, p, lj == sl ? T(0) : d);
+        drow[lj] = d;
       }
-#pragma unroll
-      for (int e = 0; e < V; ++e) {
-        const int lj = v * V + e;
-        const T dv = vget<VT, T>(d, e);
-        if (lj < lc && dv < -opt_tol) {
-          const int j = lj == sl ? lv : cvar[c0 + lj];
-          if (j < price_cols) {
-            Key kk = price_key(dv, j, c0 + lj, bland);
-            if (key_less(kk, k)) k = kk;
-          }
+      if (price && lj < lc && d < -opt_tol) {
+        const int j = lj == sl ? lv : cvar[c0 + lj];
+        if (j < price_cols) {
+          Key kk = price_key(d, j, c0 + lj, bland);
+          if (key_less(kk, k)) k = kk;
         }
       }
     }
-    k = block_min(k, redP);
+    if (!price) {  // no pricing: the pivot row only has to be visible
+      __syncthreads();
+      return k;
+    }
+    k = block_min<kW1>(k, redP);
     return cluster_min(k);
   }
 
@@ -768,7 +786,7 @@ struct Solver {
         if (key_less(kk, k)) k = kk;
       }
     }
-    k = block_min(k, redP);
+    k = block_min<kW1>(k, redP);
     return cluster_min(k);
   }
 
@@ -796,9 +814,17 @@ struct Solver {
       if (q < 0) return kOpt;
       if (pivots >= max_piv) return kUndef;
       const int s = (int)kq.w3;
-      const int owner = s / g.cw;
-      if (owner == rank) extract(g, s, c0, colbuf(cur));
-      if (CLUSTER) {
+      T theta = T(0);
+      Key kr;
+      if (!CLUSTER) {
+        // the norms are summed afresh by this pivot's sweep (the pricing
+        // reads are done: its argmin ended with a barrier); the column is
+        // extracted inside the ratio test's first pass
+        for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = 0ull;
+        kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta, s);
+      } else {
+        const int owner = s / g.cw;
+        if (owner == rank) extract(g, s, c0, colbuf(cur));
         csync();
         if (owner != rank) {
           // the column from its owner, the RHS from this CTA's own replica
@@ -809,14 +835,11 @@ struct Solver {
             rhsx[i] = tab[(size_t)i * g.ldw + g.cw];
           }
         }
+        __syncthreads();
+        for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = 0ull;
+        // ratio test: every CTA holds the column, so each computes it
+        kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta);
       }
-      __syncthreads();
-      // the norms are summed afresh by this pivot's sweep (the pricing
-      // reads above are done: barriers since)
-      for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = 0ull;
-      // ratio test: every CTA holds the column, so each computes it
-      T theta = T(0);
-      Key kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta);
       const int r = kr.w2 == ~0u ? -1 : (int)kr.w3;
       if (r < 0) return kUnbnd;
       if (theta <= deg_tol) {
@@ -888,7 +911,7 @@ struct Solver {
           if (key_less(kk, k)) k = kk;
         }
       }
-      k = block_min(k, redP);
+      k = block_min<kW1>(k, redP);
       k = cluster_min(k);
       if (CLUSTER) csync();  // pslot reads done before the next write
       if (k.w2 == ~0u) continue;  // redundant row: artificial stays basic at 0
@@ -963,7 +986,7 @@ struct Solver {
           if (key_less(kk, kr)) kr = kk;
         }
       }
-      kr = block_min(kr, redR);  // RHS replicated: every CTA finds the same row
+      kr = block_min<kW1>(kr, redR);  // RHS replicated: every CTA finds the same row
       if (kr.w2 == ~0u) return kOpt;
       if (pivots >= max_piv) return kUndef;
       const int r = (int)kr.w3;
@@ -985,7 +1008,7 @@ struct Solver {
           if (key_less(kk, kq)) kq = kk;
         }
       }
-      kq = block_min(kq, redH);
+      kq = block_min<kW1>(kq, redH);
       kq = cluster_min(kq);
       if (CLUSTER) csync();  // pslot reads done before the next cluster_min
       if (kq.w2 == ~0u) return kNoFeas;
@@ -1004,7 +1027,7 @@ struct Solver {
             }
           }
         }
-        k2 = block_min(k2, redP);
+        k2 = block_min<kW1>(k2, redP);
         kq = cluster_min(k2);
         if (CLUSTER) csync();
       }
@@ -1049,7 +1072,7 @@ struct Solver {
             }
           }
         }
-        kk = block_min(kk, redR);
+        kk = block_min<kW1>(kk, redR);
         r = kk.w2 == ~0u ? -1 : (int)kk.w3;
         if (CLUSTER && threadIdx.x == 0) sh->r = r;
       }
