@@ -1449,61 +1449,59 @@ struct Solver {
       }
     }
     __syncthreads();
-    // Tableau entries in row-major order, eight per thread per round: the
-    // round's source addresses are chosen first and its eight loads issued
-    // unconditionally (entries with no source read b[0]), so they are all in
-    // flight before the first conversion waits on one.
     const int ldw = g.ldw;
-    const int di = nt / ldw, dl = nt - di * ldw;
-    int i = tid / ldw, lj = tid - i * ldw;
-    while (i <= m) {
-      const double* src[8];
-      int at[8], kind[8];  // kind: 0 zero, 1 value, 2 negated value, 3 -1
+    // Structural block (slots [0, nA) of this CTA): a warp takes two rows at
+    // a time, each lane eight coalesced columns of each, so sixteen loads per
+    // lane are in flight before the first conversion waits on one.  Row m is
+    // the objective row (-c in a single-phase LP, 0 before phase I).
+    const int nA = max(0, min(n - c0, lc));
+    constexpr int kR = 2, kQ = 8;
+    for (int i0 = warp * kR; i0 <= m; i0 += nw * kR) {
+      for (int j0 = 0; j0 < nA; j0 += 32 * kQ) {
+        double v[kR][kQ];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        at[u] = -1;
-        kind[u] = 0;
-        src[u] = b;
-        if (i <= m) {
-          at[u] = i * ldw + lj;
-          const bool neg = i < m && na > 0 && flags[i] >= 0;
-          if (lj < lc) {
-            const int s = c0 + lj;
-            if (s < n) {
-              if (i < m) {
-                src[u] = A + (size_t)i * n + s;
-                kind[u] = neg ? 2 : 1;
-              } else if (na == 0) {
-                src[u] = c + s;
-                kind[u] = 2;
-              }
-            } else if (i < m && cvar[s] - n == i) {
-              kind[u] = 3;  // the negated row's slack
-            }
-          } else if (lj == g.cw && i < m) {
-            src[u] = b + i;
-            kind[u] = neg ? 2 : 1;
+        for (int r = 0; r < kR; ++r) {
+          const int i = i0 + r;
+          const double* src = i < m ? A + (size_t)i * n + c0 : c + c0;
+          const bool live = i < m || (i == m && na == 0);
+#pragma unroll
+          for (int q = 0; q < kQ; ++q) {
+            const int j = j0 + q * 32 + lane;
+            v[r][q] = live && j < nA ? __ldg(src + j) : 0.0;
           }
-          lj += dl;
-          i += di;
-          if (lj >= ldw) {
-            lj -= ldw;
-            ++i;
+        }
+#pragma unroll
+        for (int r = 0; r < kR; ++r) {
+          const int i = i0 + r;
+          if (i > m) continue;
+          // -c in the objective row, or a negated constraint row
+          const bool neg = i == m ? na == 0 : (na > 0 && flags[i] >= 0);
+#pragma unroll
+          for (int q = 0; q < kQ; ++q) {
+            const int j = j0 + q * 32 + lane;
+            if (j < nA) {
+              const T x = (T)v[r][q];
+              tab[(size_t)i * ldw + j] = neg ? -x : x;
+            }
           }
         }
       }
-      double raw[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) raw[u] = __ldg(src[u]);
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        if (at[u] < 0) continue;
-        T v = T(0);
-        if (kind[u] == 1) v = (T)raw[u];
-        else if (kind[u] == 2) v = -(T)raw[u];
-        else if (kind[u] == 3) v = T(-1);
-        tab[at[u]] = v;
+    }
+    // The rest of every row: slack slots of negated rows (-1 in their own
+    // row), zero padding, and the RHS (|b_i|; 0 in the objective row).
+    const int wr = ldw - nA;
+    for (int e = tid; e < (m + 1) * wr; e += nt) {
+      const int i = e / wr, lj = nA + (e - i * wr);
+      T x = T(0);
+      if (i < m) {
+        if (lj < lc) {
+          if (cvar[c0 + lj] - n == i) x = T(-1);  // the negated row's slack
+        } else if (lj == g.cw) {
+          const T bv = (T)__ldg(b + i);
+          x = (na > 0 && flags[i] >= 0) ? -bv : bv;
+        }
       }
+      tab[(size_t)i * ldw + lj] = x;
     }
     __syncthreads();
   }
