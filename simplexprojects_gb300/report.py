@@ -4,7 +4,8 @@ one workload, as JSON lines.
 For workload `kind` it times (CUDA events, device-resident data, median of
 `steps` replays) the plain FP64 tableau, the FP32 tableau with the FP64
 refresh at termination, and the FP32 tableau with periodic FP64 refreshes
-every k pivots (k in --periods), and reports for each:
+every k pivots (k in --periods), with Dantzig and with steepest-edge
+pricing, and reports for each:
   LPs/s, pivots/s, status agreement with the FP64 path, maximum relative
   objective difference to the FP64 path, and the maximum primal residual
   max_i (A x - b)_i and most negative x_j of the returned solutions.
@@ -58,9 +59,11 @@ def run(kind: int, count: int, steps: int, periods=(16, 32, 64), check: int = 25
     batch = generate(kind, count, share_family_A=True)
     out = []
     ref = None
-    modes = [("fp64", 0), ("fp32", 0)] + [("fp32", k) for k in periods]
-    for prec, period in modes:
-        db = DeviceBatch(batch, prec, want_x=True, refactor_period=period)
+    modes = ([("fp64", 0, "dantzig"), ("fp32", 0, "dantzig")]
+             + [("fp32", k, "dantzig") for k in periods]
+             + [("fp32", 0, "steepest")] + [("fp32", k, "steepest") for k in periods])
+    for prec, period, pricing in modes:
+        db = DeviceBatch(batch, prec, want_x=True, refactor_period=period, pricing=pricing)
         ms = _time(db, steps)
         r = db.result()
         if ref is None:
@@ -70,6 +73,7 @@ def run(kind: int, count: int, steps: int, periods=(16, 32, 64), check: int = 25
         sub = batch.head(min(check, batch.count))
         res, neg = residuals(sub, r.x)
         out.append(dict(workload=kind, lps=batch.count, precision=prec, refresh_period=period,
+                        pricing=pricing,
                         ms=ms, lps_per_s=batch.count / (ms * 1e-3),
                         pivots_per_s=float(r.pivots.sum()) / (ms * 1e-3),
                         mean_pivots=float(r.pivots.mean()),
