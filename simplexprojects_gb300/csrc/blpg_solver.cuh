@@ -1564,7 +1564,10 @@ struct Solver {
       load(g, c0, lc, A, b, c);
       int pivots = 0, degen = 0, cur = 0, st, info = 0;
       const float* w = a.weight ? a.weight + a.offw[lp] : nullptr;
-      bool bland = false, refreshed = false;
+      bool bland = false;
+      // pivot count at the last FP64 refresh: its x_B and objective are
+      // reported only if no pivot followed it (-1: none yet)
+      int piv_fresh = -1;
       const int max_piv = a.max_pivots > 0 ? a.max_pivots : 50 * (m + n) + 1000;
       const T ptol = (T)a.ptol, opt_tol = (T)a.opt_tol;
       if (na > 0) {
@@ -1598,7 +1601,7 @@ struct Solver {
             info |= kInfoFallback;
             if (CLUSTER) csync();
             load(g, c0, lc, A, b, c);
-            refreshed = false;
+            piv_fresh = -1;
             bland = false;
             degen = 0;
             budget = pivots + max_piv;
@@ -1641,7 +1644,7 @@ struct Solver {
               info |= kInfoFallback;
               if (CLUSTER) csync();
               load(g, c0, lc, A, b, c);
-              refreshed = false;
+              piv_fresh = -1;
               bland = false;
               degen = 0;
               st = -1;
@@ -1654,7 +1657,7 @@ struct Solver {
               if (st != kRefresh) break;
               if (CLUSTER) csync();
               refresh(g, A, b, c, a);
-              refreshed = true;
+              piv_fresh = pivots;
               info |= kInfoRefresh;
             }
           }
@@ -1665,7 +1668,7 @@ struct Solver {
             for (int round = 0; round <= 4; ++round) {
               if (CLUSTER) csync();
               const int fl = refresh(g, A, b, c, a);
-              refreshed = true;
+              piv_fresh = pivots;
               info |= kInfoRefresh;
               if (!(fl & 4)) break;  // refinement did not converge
               if ((fl & 3) == 3) {
@@ -1692,7 +1695,16 @@ struct Solver {
           st = kUndef;
           info |= kInfoUnverified;
         }
+        // FP32 unbounded: x_B of the final basis (where unboundedness was
+        // found) from the FP64 refresh too, not from the FP32 tableau
+        if (kFP32 && st == kUnbnd && piv_fresh != pivots) {
+          if (CLUSTER) csync();
+          refresh(g, A, b, c, a);
+          piv_fresh = pivots;
+          info |= kInfoRefresh;
+        }
       }
+      const bool refreshed = piv_fresh == pivots;
       if (CLUSTER) csync();
       // outputs (rank 0 holds a replica of the RHS column; after an FP64
       // refresh the FP64 x_B and objective are reported)

@@ -43,10 +43,13 @@ def _time(db, steps, warmup=2):
     return statistics.median(a.elapsed_time(b) for a, b in ev)
 
 
-def residuals(batch, x):
-    """(max_i (A x - b)_i over all LPs, min_j x_j) of solutions x (off_c layout)."""
+def residuals(batch, x, status=None):
+    """(max_i (A x - b)_i, min_j x_j) over the LPs of a batch whose status is
+    optimal (all LPs when no status is given); x in the off_c layout."""
     worst, neg = -np.inf, np.inf
     for k in range(batch.count):
+        if status is not None and status[k] != 5:
+            continue
         A, b, _ = batch.lp(k)
         _, _, oc = batch.offsets()
         xk = x[oc[k]:oc[k] + A.shape[1]]
@@ -71,7 +74,7 @@ def run(kind: int, count: int, steps: int, periods=(16, 32, 64), check: int = 25
         ok = ref.status == 5
         rel = np.abs(r.objective[ok] - ref.objective[ok]) / np.maximum(np.abs(ref.objective[ok]), 1.0)
         sub = batch.head(min(check, batch.count))
-        res, neg = residuals(sub, r.x)
+        res, neg = residuals(sub, r.x, r.status)
         out.append(dict(workload=kind, lps=batch.count, precision=prec, refresh_period=period,
                         pricing=pricing,
                         ms=ms, lps_per_s=batch.count / (ms * 1e-3),

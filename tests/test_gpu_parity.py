@@ -195,3 +195,23 @@ def test_empty_batch_and_errors(built):
     with pytest.raises(sp._native.BlpgError) as e:
         sp.solve(big)
     assert e.value.code == -5
+
+
+@pytest.mark.parametrize("kind,period", [(1, 0), (1, 16), (4, 16)])
+def test_fp32_solutions_are_feasible(built, kind, period):
+    """The x reported in FP32 mode belongs to the final basis: FP64-refreshed,
+    so Ax <= b and x >= 0 hold to rounding for optimal LPs and for the basic
+    solution where unboundedness was found (with periodic refreshes the last
+    refresh may precede later pivots, and its x must not be reported)."""
+    batch = sp.generate(kind, 512, seed=41 + kind)
+    g = sp.solve(batch, "fp32", refactor_period=period, want_x=True)
+    _, _, oc = batch.offsets()
+    for k in range(batch.count):
+        if g.status[k] not in (5, 6):
+            continue
+        A, b, _ = batch.lp(k)
+        xk = g.x[oc[k]:oc[k] + A.shape[1]]
+        # the FP64 check accepts x_B >= -1e-7 (the FP32 mode's primal tolerance)
+        scale = max(1.0, float(np.abs(b).max()), float(np.abs(xk).max()))
+        assert (A @ xk - b).max() <= 1e-7 * scale, (k, g.status[k])
+        assert xk.min() >= -1e-7 * scale, (k, g.status[k])
