@@ -62,9 +62,7 @@ def workload(kind: int, rank: int = 0, world: int = 1):
         count, first = 10_000, 40_000  # the evaluation split
     else:
         count, first = sp.WORKLOAD_COUNTS[kind], 0
-    per = (count + world - 1) // world
-    lo = first + rank * per
-    n = max(0, min(per, first + count - lo))
+    lo, n = sp.shard(count, first, rank, world)
     return sp.generate(kind, n, seed=sp.DEFAULT_SEED, first=lo, share_family_A=True), count
 
 
@@ -175,7 +173,7 @@ def run_reference(args, rank, world):
     }))
 
 
-def run_learned(args, rank, world, local):
+def run_learned(args, rank, world, local, dist=None):
     """Workload 3: the learned warm start + FP32 tableau on the 10,000
     evaluation LPs, against the plain FP64 cold solver on the same LPs."""
     import torch
@@ -186,9 +184,7 @@ def run_learned(args, rank, world, local):
 
     dev = f"cuda:{local}"
     t_setup = time.perf_counter()
-    per = (10_000 + world - 1) // world
-    lo = 40_000 + rank * per
-    n_eval = max(0, min(per, 50_000 - lo))
+    lo, n_eval = sp.shard(10_000, 40_000, rank, world)
     train = sp.generate(3, 40_000, seed=sp.DEFAULT_SEED, first=0, share_family_A=True)
     evalb = sp.generate(3, n_eval, seed=sp.DEFAULT_SEED, first=lo, share_family_A=True)
     tb = sp.solve(train, "fp64", want_basis=True)  # plain FP64 solver labels its own bases
@@ -216,15 +212,29 @@ def run_learned(args, rank, world, local):
         torch.cuda.synchronize()
         return [a.elapsed_time(b) for a, b in ev]
 
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(v: float) -> float:
+        """Whole-job time: the slowest rank's."""
+        if dist is None:
+            return v
+        t = torch.tensor([v], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
     for _ in range(args.warmup):
         ls.run()
         plain.run()
     torch.cuda.synchronize()
     with Clocks(local) as clk:
+        barrier()
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_push("timed_region")
         t_learned = timed(ls.run, args.steps)
         torch.cuda.nvtx.range_pop()
+        barrier()
     t_plain = timed(plain.run, args.steps)
     ls.predict()
     t_solve = timed(lambda: ls.db.run(weight=ls.weight), args.steps)  # the FP32 solve alone
@@ -237,7 +247,8 @@ def run_learned(args, rank, world, local):
                           ("cold_fp32_steepest", cold32se.run, cold32se)):
         for _ in range(2):
             fn()
-        tv = statistics.median(timed(fn, max(3, args.steps // 2)))
+        barrier()
+        tv = max_over_ranks(statistics.median(timed(fn, max(3, args.steps // 2))))
         rv = obj.result()
         variants[name] = {"value": len(rv.status) * world / (tv * 1e-3), "unit": "LPs/s",
                           "ms_per_step": tv, "mean_pivots": float(rv.pivots.mean()),
@@ -246,19 +257,20 @@ def run_learned(args, rank, world, local):
     hint = crash.hint.cpu().numpy()
     plain_b = sp.solve(evalb, "fp64", want_basis=True)
     acc, exact = basis_accuracy(hint, plain_b.basis, 174)
-    ms = statistics.median(t_learned)
-    ms_plain = statistics.median(t_plain)
-    ms_solve = statistics.median(t_solve)
+    ms = max_over_ranks(statistics.median(t_learned))
+    ms_plain = max_over_ranks(statistics.median(t_plain))
+    ms_solve = max_over_ranks(statistics.median(t_solve))
     ok = pres.status == 5
     rel = np.abs(res.objective[ok] - pres.objective[ok]) / np.maximum(np.abs(pres.objective[ok]), 1.0)
     # e2e through the public call from host arrays
     e2e = []
     for i in range(args.warmup + args.steps):
+        barrier()
         t0 = time.perf_counter()
         r2 = ls.solve(evalb)
         if i >= args.warmup:
             e2e.append(time.perf_counter() - t0)
-    e2e_ms = statistics.median(e2e) * 1e3
+    e2e_ms = max_over_ranks(statistics.median(e2e) * 1e3)
     assert np.array_equal(r2.status, res.status)
     if rank != 0:
         return
@@ -356,7 +368,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     if args.workload == 3:
-        run_learned(args, rank, world, local)
+        run_learned(args, rank, world, local, dist)
         if dist is not None:
             dist.destroy_process_group()
         return

@@ -9,12 +9,12 @@ Public API:
 """
 from . import _native
 from ._native import BlpgError
-from .lp import LPBatch, generate, read_abc, WORKLOAD_COUNTS, DEFAULT_SEED
+from .lp import LPBatch, generate, read_abc, shard, WORKLOAD_COUNTS, DEFAULT_SEED
 from .solver import DeviceBatch, Plan, Simplex, SolveResult, options, solve
 
 __all__ = [
     "LPBatch", "generate", "read_abc", "solve", "Plan", "DeviceBatch", "Simplex", "SolveResult",
-    "options", "WORKLOAD_COUNTS", "DEFAULT_SEED", "BlpgError",
+    "options", "WORKLOAD_COUNTS", "DEFAULT_SEED", "BlpgError", "shard",
 ]
 
 

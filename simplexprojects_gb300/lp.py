@@ -127,6 +127,16 @@ class LPBatch:
                    off_c=np.arange(k, dtype=np.int64) * n)
 
 
+def shard(count: int, first: int, rank: int, world: int):
+    """(first LP index, LP count) of rank `rank` of `world` over LPs
+    first .. first + count - 1: contiguous blocks of ceil(count / world), the
+    last rank taking the remainder.  LPs are independent, so a multi-GPU run
+    solves one shard per GPU and needs no collective on the data path."""
+    per = (count + world - 1) // world
+    lo = first + rank * per
+    return lo, max(0, min(per, first + count - lo))
+
+
 def generate(kind: int, count: Optional[int] = None, seed: int = DEFAULT_SEED, first: int = 0,
              threads: int = 0, share_family_A: bool = False) -> LPBatch:
     """Synthetic workload `kind` (0..4, see include/blpg.h): LPs first ..
