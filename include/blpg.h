@@ -231,8 +231,9 @@ void blpg_plan_destroy(blpg_plan* plan);
 /* Size-class table (JSON text, as written by the autotuner): overrides the
  * built-in heuristic for threads per CTA ("fp64_k1": 256, per precision and
  * cluster size), the per-CTA shared-memory budget ("fp32_smem": bytes) and
- * the CTAs per SM target ("fp32_ctas": 2; default: as many as shared memory
- * admits).  Null resets. */
+ * the cap on CTAs per SM for single-CTA LPs ("fp32_ctas": 2; default: as
+ * many as shared memory admits, at most 16 in FP32 and 4 in FP64).  Null
+ * resets. */
 int32_t blpg_set_tuning(const char* json_text);
 
 const char* blpg_last_error(void);

@@ -238,8 +238,12 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
   const int se = p->opt.pricing == BLPG_PRICE_STEEPEST ? 1 : 0;
   const int min_cluster = std::max(1, std::min(p->opt.min_cluster, max_cluster));
   constexpr int kMaxCtasPerSm = 16;
+  // default cap, from the autotuner on the uneven workload (GB300): FP64 small
+  // LPs are bound by the FP64 pipe, so more than 4 CTAs per SM only lengthen
+  // each LP (4 is 5 % faster than 16); FP32 gains up to 16
+  const int cps_default = p->precision == BLPG_FP64 ? 4 : kMaxCtasPerSm;
   const int cps_cap =
-      std::max(1, std::min(kMaxCtasPerSm, tuning_value(p->precision * 16 + 14, 2, kMaxCtasPerSm)));
+      std::max(1, std::min(kMaxCtasPerSm, tuning_value(p->precision * 16 + 14, 2, cps_default)));
   auto cta_limit = [&](int cps) {  // per-CTA shared memory for cps CTAs per SM
     return std::min(max_smem, p->smem_per_sm / cps - p->smem_reserved);
   };
