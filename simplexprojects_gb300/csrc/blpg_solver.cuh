@@ -315,12 +315,39 @@ __device__ __forceinline__ float4 v_fma(float f, const float4& p, const float4& 
   return make_float4(fmaf(-f, p.x, t.x), fmaf(-f, p.y, t.y), fmaf(-f, p.z, t.z),
                      fmaf(-f, p.w, t.w));
 }
-__device__ __forceinline__ double2 v_sq(const double2& t, const double2& a) {
-  return make_double2(fma(t.x, t.x, a.x), fma(t.y, t.y, a.y));
+// Steepest-edge norm accumulation.  Pricing only needs the norms' size, so
+// an FP64 value enters as an FP32 approximation of its magnitude built from
+// its exponent and top 20 mantissa bits with integer operations (values
+// below FLT_MIN count as 0, above FLT_MAX as FLT_MAX): the squares then run
+// on the FP32 pipe, not GB300's slow FP64 pipe.  FP32 values are squared as
+// they are.
+__device__ __forceinline__ float mag_f32(double x) {
+  const unsigned hi = (unsigned)((unsigned long long)__double_as_longlong(x) >> 32) & 0x7FFFFFFFu;
+  const int e = (int)(hi >> 20) - 896;  // biased FP32 exponent
+  const unsigned bits = ((unsigned)e << 23) | ((hi & 0xFFFFFu) << 3);
+  return e <= 0 ? 0.f : (e >= 255 ? 3.4e38f : __uint_as_float(bits));
+}
+template <typename T>
+struct SqT;
+template <>
+struct SqT<double> {
+  using type = float2;
+};
+template <>
+struct SqT<float> {
+  using type = float4;
+};
+__device__ __forceinline__ float2 v_sq(const double2& t, const float2& a) {
+  const float x = mag_f32(t.x), y = mag_f32(t.y);
+  return make_float2(fmaf(x, x, a.x), fmaf(y, y, a.y));
 }
 __device__ __forceinline__ float4 v_sq(const float4& t, const float4& a) {
   return make_float4(fmaf(t.x, t.x, a.x), fmaf(t.y, t.y, a.y), fmaf(t.z, t.z, a.z),
                      fmaf(t.w, t.w, a.w));
+}
+__device__ __forceinline__ float sq_get(const float2& a, int e) { return e == 0 ? a.x : a.y; }
+__device__ __forceinline__ float sq_get(const float4& a, int e) {
+  return e == 0 ? a.x : (e == 1 ? a.y : (e == 2 ? a.z : a.w));
 }
 __device__ __forceinline__ double2 v_div(const double2& a, double d) {
   return make_double2(a.x / d, a.y / d);
@@ -615,7 +642,7 @@ struct Solver {
     bool zs[V];
 #pragma unroll
     for (int e = 0; e < V; ++e) zs[e] = has_s && se == e;
-    VT sq = VT{};  // steepest edge: sum of squares of this lane's final values
+    typename SqT<T>::type sq{};  // steepest edge: sum of squares of this lane's final values
     // One row: the elimination is computed unconditionally and stored only
     // where it applies (a zero multiplier leaves the row as it is; row r
     // already holds the divided pivot row), so the body has no divergent
@@ -658,7 +685,7 @@ struct Solver {
       for (int e2 = 0; e2 < V; ++e2) {
         const int e = (e2 + (lane >> 2)) & (V - 1);
         const int lj = lane * V + e;
-        if (lj < lc) atomicAdd(&gam[lj], norm_fixed(vget<VT, T>(sq, e)));
+        if (lj < lc) atomicAdd(&gam[lj], norm_fixed(sq_get(sq, e)));
       }
     }
     if (has_q && grp == 0) colx_next[m] = tb[(size_t)m * ldw + qloc];
@@ -746,13 +773,13 @@ struct Solver {
     const int nt = (int)blockDim.x, G = nt / g.nl;
     const int grp = threadIdx.x / g.nl, lane = threadIdx.x - grp * g.nl;
     if (grp < G) {
-      VT sq = VT{};
+      typename SqT<T>::type sq{};
       for (int i = grp; i < g.m; i += G)
         sq = v_sq(*reinterpret_cast<const VT*>(tab + (size_t)i * g.ldw + lane * V), sq);
 #pragma unroll
       for (int e = 0; e < V; ++e) {
         const int lj = lane * V + e;
-        if (lj < lc) atomicAdd(&gam[lj], norm_fixed(vget<VT, T>(sq, e)));
+        if (lj < lc) atomicAdd(&gam[lj], norm_fixed(sq_get(sq, e)));
       }
     }
     __syncthreads();
