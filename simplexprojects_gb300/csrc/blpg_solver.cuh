@@ -486,15 +486,18 @@ struct Solver {
   // performs the same operations.
   // With fuse_sl >= 0 the entering column (local slot fuse_sl) and the RHS
   // are read from the tableau and copied into colx / rhsx on the way, the
-  // first pass's barrier publishing them (single-CTA steepest-edge loop).
+  // first pass's barrier publishing them (single-CTA steepest-edge loop);
+  // with zero_sl the tableau's slot is also cleared in rows 0..m-1, as the
+  // FP32 steepest-edge sweep expects.
   __device__ Key ratio(const Geom& g, T* colx, T piv_tol, T feas_tol, bool harris, T& theta,
-                       int fuse_sl = -1) {
+                       int fuse_sl = -1, bool zero_sl = false) {
     auto fetch = [&](int i, T& a, T& rh) {
       if (fuse_sl >= 0) {
         a = tab[(size_t)i * g.ldw + fuse_sl];
         rh = tab[(size_t)i * g.ldw + g.cw];
         colx[i] = a;
         rhsx[i] = rh;
+        if (zero_sl) tab[(size_t)i * g.ldw + fuse_sl] = T(0);
       } else {
         a = colx[i];
         rh = rhsx[i];
@@ -613,12 +616,20 @@ struct Solver {
     update_rows<true>(tab, rhsx, rank, g.m, g.ldw, g.nl, g.cw, r, s, pcol, -1, -1, c0, nullptr,
                       gam, lc);
   }
+  // The FP32 single-CTA steepest-edge sweep: the entering slot was cleared
+  // by the ratio test and fcol is the pivot column with row r's entry 0, so
+  // every row is t + f * p, stored where f != 0.  A row with f == 0 computes
+  // t back (p is finite), so the norms take every computed row as it is.
+  __device__ void update_body_se32(const Geom& g, int r, const T* fcol, int lc) {
+    update_rows<true, true>(tab, rhsx, rank, g.m, g.ldw, g.nl, g.cw, r, -1, fcol, -1, -1, 0,
+                            nullptr, gam, lc);
+  }
   // Kept out of line with plain arguments (no `this`, no structs by
   // reference) so that the unrolled sweep has its own register budget and
   // nothing in its loop lives in local memory.  The slot s entry of every
   // updated row is taken as 0 before the elimination (it held the entering
   // column, whose slot now carries the leaving variable's unit column).
-  template <bool SE>
+  template <bool SE, bool PRE = false>
   static __device__ __noinline__ void update_rows(T* const tb, T* const rhsx, const int rank,
                                                   const int m, const int ldw, const int nl,
                                                   const int cw, const int r, const int s,
@@ -648,6 +659,14 @@ struct Solver {
     // already holds the divided pivot row), so the body has no divergent
     // branch, only predicated stores.
     auto row = [&](const int i, const T f, const VT t) {
+      if constexpr (PRE) {
+        // slot s and row r were prepared by the caller
+        const VT tn = v_fma(f, p, t);
+        if (f != T(0)) *reinterpret_cast<VT*>(tb + (size_t)i * ldw + lane * V) = tn;
+        if (has_rhs) rhsx[i] = vget<VT, T>(tn, 0);
+        sq = v_sq(tn, sq);
+        return;
+      }
       const bool upd = f != T(0) && i != r;
       VT tz = t;
 #pragma unroll
@@ -834,6 +853,8 @@ struct Solver {
                          int& cur, int period = 0) {
     const T opt_tol = (T)a.opt_tol, piv_tol = (T)a.piv_tol, feas_tol = (T)a.feas_tol;
     const T deg_tol = (T)a.deg_tol;
+    // FP32 on one CTA: the sweep with the entering slot and row r prepared
+    constexpr bool kPre = sizeof(T) == 4 && !CLUSTER;
     norms_full(g, lc);
     for (;;) {
       Key kq = price_se(g, c0, lc, bland, opt_tol, price_cols, w);
@@ -846,9 +867,9 @@ struct Solver {
       if (!CLUSTER) {
         // the norms are summed afresh by this pivot's sweep (the pricing
         // reads are done: its argmin ended with a barrier); the column is
-        // extracted inside the ratio test's first pass
+        // extracted inside the ratio test's first pass (FP32: and cleared)
         for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = 0ull;
-        kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta, s);
+        kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta, s, kPre);
       } else {
         const int owner = s / g.cw;
         if (owner == rank) extract(g, s, c0, colbuf(cur));
@@ -868,7 +889,14 @@ struct Solver {
         kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta);
       }
       const int r = kr.w2 == ~0u ? -1 : (int)kr.w3;
-      if (r < 0) return kUnbnd;
+      if (r < 0) {
+        if (kPre) {  // the entering column goes back where the ratio test cleared it
+          for (int i = threadIdx.x; i < g.m; i += blockDim.x)
+            tab[(size_t)i * g.ldw + s] = colbuf(cur)[i];
+          __syncthreads();
+        }
+        return kUnbnd;
+      }
       if (theta <= deg_tol) {
         if (++degen > a.bland_after) bland = true;
       } else {
@@ -876,9 +904,18 @@ struct Solver {
       }
       const T* pcol = colbuf(cur);
       const int lv = basis[r];
+      if (kPre) {
+        // the sweep's multipliers: the pivot column with row r's entry 0
+        // (published by the pivot row's barrier)
+        T* fcol = colbuf(cur ^ 1);
+        for (int i = threadIdx.x; i < g.m; i += blockDim.x) fcol[i] = i == r ? T(0) : pcol[i];
+      }
       pivot_rows(g, r, s, lv, pcol, c0, lc, false, T(0), 0);
       relabel(r, s, q, lv);
-      update_body_se(g, r, s, pcol, c0, lc);
+      if (kPre)
+        update_body_se32(g, r, colbuf(cur ^ 1), lc);
+      else
+        update_body_se(g, r, s, pcol, c0, lc);
       __syncthreads();
       ++pivots;
       if (pivots >= max_piv) return kUndef;
