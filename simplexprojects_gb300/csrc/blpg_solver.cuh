@@ -327,6 +327,30 @@ __device__ __forceinline__ float mag_f32(double x) {
   const unsigned bits = ((unsigned)e << 23) | ((hi & 0xFFFFFu) << 3);
   return e <= 0 ? 0.f : (e >= 255 ? 3.4e38f : __uint_as_float(bits));
 }
+// FP64 -> FP32 rounded to nearest even, built with integer operations (the
+// FP64-to-FP32 conversion instruction runs at GB300's low FP64 rate).  A
+// funnel shift of the two halves left by 3 puts the low 8 bits of the FP64
+// exponent e and the top 23 fraction bits where FP32 keeps its exponent and
+// fraction; for e in [897, 1149] the FP32 exponent e - 896 equals those 8
+// bits with the top one flipped.  The 29 dropped bits round up above one half
+// and at one half when the kept bits are odd: their sum with 2^28 - 1 plus
+// the kept lowest bit carries out of bit 29 exactly then (a carry into the
+// exponent is the correctly rounded result).  FP64 zeros and subnormals (far
+// below FP32's smallest subnormal) become zeros of their sign; only results
+// below FP32's normal range and values near or above its maximum take the
+// conversion instruction.
+__device__ __forceinline__ float f64_to_f32_rn(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned e = (hi >> 20) & 0x7FFu;
+  unsigned bits = (__funnelshift_l(lo, hi, 3) & 0x7FFFFFFFu) ^ 0x40000000u;
+  bits += ((lo & 0x1FFFFFFFu) + 0x0FFFFFFFu + (bits & 1u)) >> 29;
+  if (e - 897u < 253u) return __uint_as_float(bits | (hi & 0x80000000u));
+  if (e == 0u) return __uint_as_float(hi & 0x80000000u);
+  return (float)x;
+}
+__device__ __forceinline__ float to_tab(double x, float) { return f64_to_f32_rn(x); }
+__device__ __forceinline__ double to_tab(double x, double) { return x; }
+
 template <typename T>
 struct SqT;
 template <>
@@ -357,18 +381,25 @@ __device__ __forceinline__ float4 v_div(const float4& a, float d) {
                      __fdiv_rn(a.w, d));
 }
 
-// Steepest-edge column norms are summed as 64-bit fixed-point integers with
-// 2^-24 resolution (shared-memory atomics; integer sums do not depend on the
-// order of the additions).  gamma_j = 1 + sum_i T_ij^2.  A partial sum is
-// clamped to 2^30 so that no total can overflow.
-__device__ __forceinline__ unsigned long long norm_fixed(float v) {
-  return __float2ull_rn(fminf(v, 1073741824.f) * 16777216.f);
+// Steepest-edge column norms gamma_j = 1 + sum_i T_ij^2 are summed as
+// fixed-point integers with 2^-24 resolution, in two 32-bit shared counters
+// per column (x: the 24-bit fractions, y: the integer parts): integer sums do
+// not depend on the order of the additions, and a 32-bit shared atomic add
+// is one instruction where a 64-bit one is a compare-and-swap loop.  At most
+// kMaxNormGroups partial sums reach a column, each clamped to 2^25, so the
+// integer counter stays below 2^31 and the fraction counter below 2^30.
+constexpr int kMaxNormGroups = 64;
+// The two parts of RN(v * 2^24) come from 32-bit conversions: v * 2^24 is
+// exact, an integer from v = 1/2 up, so truncating v gives the integer part
+// exactly and the remainder v - trunc(v) is exact too.
+__device__ __forceinline__ void norm_add(uint2* gcol, float v) {
+  v = fminf(v, 33554432.f);
+  const unsigned ip = __float2uint_rz(v);
+  atomicAdd(&gcol->x, __float2uint_rn((v - (float)ip) * 16777216.f));
+  atomicAdd(&gcol->y, ip);
 }
-__device__ __forceinline__ unsigned long long norm_fixed(double v) {
-  return __double2ull_rn(fmin(v, 1073741824.0) * 16777216.0);
-}
-__device__ __forceinline__ double norm_value(unsigned long long u) {
-  return 1.0 + (double)u * (1.0 / 16777216.0);
+__device__ __forceinline__ float norm_gamma(uint2 gv) {
+  return 1.f + ((float)gv.y + (float)gv.x * (1.f / 16777216.f));
 }
 
 // Status codes (GLPK numbering, as blpg.h)
@@ -412,7 +443,7 @@ struct Solver {
   int* flags;
   int* cvar;   // slot -> variable id (every slot of the LP, replicated per CTA)
   int* vpos;   // variable -> slot if nonbasic, -1 - row if basic
-  unsigned long long* gam;  // steepest edge: fixed-point column norms of the local slots
+  uint2* gam;  // steepest edge: fixed-point column norms of the local slots
   double* xr;  // FP32 tableau only: FP64 x_B of the refresh
   double* yr;  // FP32 tableau only: FP64 duals of the refresh
   float* rf;   // FP32 tableau only: the refresh's residuals rounded to FP32
@@ -635,9 +666,9 @@ struct Solver {
                                                   const int cw, const int r, const int s,
                                                   const T* pcol, const int qn, const int owner_n,
                                                   const int c0, T* colx_next,
-                                                  unsigned long long* gam, const int lc) {
+                                                  uint2* gam, const int lc) {
     const int nt = (int)blockDim.x;
-    const int G = nt / nl;
+    const int G = SE ? min(nt / nl, kMaxNormGroups) : nt / nl;  // rows of lanes
     const int grp = threadIdx.x / nl;
     const int lane = threadIdx.x - grp * nl;
     if (grp >= G) return;
@@ -704,7 +735,7 @@ struct Solver {
       for (int e2 = 0; e2 < V; ++e2) {
         const int e = (e2 + (lane >> 2)) & (V - 1);
         const int lj = lane * V + e;
-        if (lj < lc) atomicAdd(&gam[lj], norm_fixed(sq_get(sq, e)));
+        if (lj < lc) norm_add(&gam[lj], sq_get(sq, e));
       }
     }
     if (has_q && grp == 0) colx_next[m] = tb[(size_t)m * ldw + qloc];
@@ -787,9 +818,9 @@ struct Solver {
   // recomputed with a full pass (at the start of a pricing loop, after
   // loads, crashes, refreshes and pivots made without norms).
   __device__ void norms_full(const Geom& g, int lc) {
-    for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = 0ull;
+    for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = make_uint2(0u, 0u);
     __syncthreads();
-    const int nt = (int)blockDim.x, G = nt / g.nl;
+    const int nt = (int)blockDim.x, G = min(nt / g.nl, kMaxNormGroups);
     const int grp = threadIdx.x / g.nl, lane = threadIdx.x - grp * g.nl;
     if (grp < G) {
       typename SqT<T>::type sq{};
@@ -798,7 +829,7 @@ struct Solver {
 #pragma unroll
       for (int e = 0; e < V; ++e) {
         const int lj = lane * V + e;
-        if (lj < lc) atomicAdd(&gam[lj], norm_fixed(sq_get(sq, e)));
+        if (lj < lc) norm_add(&gam[lj], sq_get(sq, e));
       }
     }
     __syncthreads();
@@ -820,10 +851,7 @@ struct Solver {
         if (bland) {
           kk = price_key(v, j, c0 + lj, true);
         } else {
-          const unsigned long long u = gam[lj];
-          const float gm =
-              1.f + ((float)(unsigned)(u >> 32) * 4294967296.f + (float)(unsigned)u) *
-                        (1.f / 16777216.f);
+          const float gm = norm_gamma(gam[lj]);
           const float vf = (float)v;
           float sc = __fdividef(vf * vf, gm);
           if (w) sc *= w[j];
@@ -868,7 +896,7 @@ struct Solver {
         // the norms are summed afresh by this pivot's sweep (the pricing
         // reads are done: its argmin ended with a barrier); the column is
         // extracted inside the ratio test's first pass (FP32: and cleared)
-        for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = 0ull;
+        for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = make_uint2(0u, 0u);
         kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta, s, kPre);
       } else {
         const int owner = s / g.cw;
@@ -884,7 +912,7 @@ struct Solver {
           }
         }
         __syncthreads();
-        for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = 0ull;
+        for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = make_uint2(0u, 0u);
         // ratio test: every CTA holds the column, so each computes it
         kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta);
       }
@@ -1456,6 +1484,84 @@ struct Solver {
     return ok;
   }
 
+  // The structural block of the tableau from rows of A (Ac = A's column
+  // c0 of row 0, cc = c + c0): a warp takes two rows at a time, each lane
+  // eight coalesced columns of each, so that sixteen loads per lane are in
+  // flight before the first conversion waits on one.  Out of line with plain
+  // arguments, so that its registers do not add to the kernel's.
+  static __device__ __noinline__ void load_block(T* __restrict__ const tb,
+                                                 const double* __restrict__ const Ac,
+                                                 const double* __restrict__ const cc,
+                                                 const int* __restrict__ const flags,
+                                                 const int m, const int n, const int nA,
+                                                 const int ldw, const int na) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    constexpr int kR = 2, kQ = 8;
+    for (int i0 = warp * kR; i0 <= m; i0 += nw * kR) {
+      for (int j0 = 0; j0 < nA; j0 += 32 * kQ) {
+        double v[kR][kQ];
+#pragma unroll
+        for (int r = 0; r < kR; ++r) {
+          const int i = i0 + r;
+          const double* src = i < m ? Ac + (size_t)i * n : cc;
+          const bool live = i < m || (i == m && na == 0);
+#pragma unroll
+          for (int q = 0; q < kQ; ++q) {
+            const int j = j0 + q * 32 + lane;
+            v[r][q] = live && j < nA ? __ldg(src + j) : 0.0;
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < kR; ++r) {
+          const int i = i0 + r;
+          if (i > m) continue;
+          // -c in the objective row, or a negated constraint row
+          const bool neg = i == m ? na == 0 : (na > 0 && flags[i] >= 0);
+#pragma unroll
+          for (int q = 0; q < kQ; ++q) {
+            const int j = j0 + q * 32 + lane;
+            if (j < nA) {
+              const T x = to_tab(v[r][q], T(0));
+              tb[(size_t)i * ldw + j] = neg ? -x : x;
+            }
+          }
+        }
+      }
+    }
+  }
+
+  // FP64 tableau: the structural block copied straight from rows of A (and
+  // c for row m of a single-phase LP) by asynchronous 8-byte global-to-shared
+  // copies, which need no registers, then the rows to negate negated in place.
+  __device__ void load_rows_async(const Geom& g, int c0, int nA, const double* A,
+                                  const double* c) {
+    const int m = g.m, n = g.n, na = g.na, ldw = g.ldw;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = warp; i <= m; i += nw) {
+      T* dst = tab + (size_t)i * ldw;
+      if (i == m && na > 0) {  // phase I starts from a zero objective row
+        for (int j = lane; j < nA; j += 32) dst[j] = T(0);
+        continue;
+      }
+      const double* src = i < m ? A + (size_t)i * n + c0 : c + c0;
+      for (int j = lane; j < nA; j += 32) {
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + j);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(src + j)
+                     : "memory");
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+    // -c in the objective row of a single-phase LP; the rows with b_i < 0
+    for (int i = warp; i <= m; i += nw) {
+      const bool neg = i == m ? na == 0 : (na > 0 && flags[i] >= 0);
+      if (!neg) continue;
+      T* row = tab + (size_t)i * ldw;
+      for (int j = lane; j < nA; j += 32) row[j] = -row[j];
+    }
+  }
+
   // Build the slack-basis tableau of LP lp: rows with b_i < 0 are negated
   // and get an artificial variable each (the a-th such row's artificial is
   // basic there and its slack takes column slot n + a); structural j sits in
@@ -1514,43 +1620,13 @@ struct Solver {
     }
     __syncthreads();
     const int ldw = g.ldw;
-    // Structural block (slots [0, nA) of this CTA): a warp takes two rows at
-    // a time, each lane eight coalesced columns of each, so sixteen loads per
-    // lane are in flight before the first conversion waits on one.  Row m is
-    // the objective row (-c in a single-phase LP, 0 before phase I).
+    // Structural block (slots [0, nA) of this CTA); row m is the objective
+    // row (-c in a single-phase LP, 0 before phase I)
     const int nA = max(0, min(n - c0, lc));
-    constexpr int kR = 2, kQ = 8;
-    for (int i0 = warp * kR; i0 <= m; i0 += nw * kR) {
-      for (int j0 = 0; j0 < nA; j0 += 32 * kQ) {
-        double v[kR][kQ];
-#pragma unroll
-        for (int r = 0; r < kR; ++r) {
-          const int i = i0 + r;
-          const double* src = i < m ? A + (size_t)i * n + c0 : c + c0;
-          const bool live = i < m || (i == m && na == 0);
-#pragma unroll
-          for (int q = 0; q < kQ; ++q) {
-            const int j = j0 + q * 32 + lane;
-            v[r][q] = live && j < nA ? __ldg(src + j) : 0.0;
-          }
-        }
-#pragma unroll
-        for (int r = 0; r < kR; ++r) {
-          const int i = i0 + r;
-          if (i > m) continue;
-          // -c in the objective row, or a negated constraint row
-          const bool neg = i == m ? na == 0 : (na > 0 && flags[i] >= 0);
-#pragma unroll
-          for (int q = 0; q < kQ; ++q) {
-            const int j = j0 + q * 32 + lane;
-            if (j < nA) {
-              const T x = (T)v[r][q];
-              tab[(size_t)i * ldw + j] = neg ? -x : x;
-            }
-          }
-        }
-      }
-    }
+    if constexpr (sizeof(T) == 8)
+      load_rows_async(g, c0, nA, A, c);
+    else
+      load_block(tab, A + c0, c + c0, flags, m, n, nA, ldw, na);
     // The rest of every row: slack slots of negated rows (-1 in their own
     // row), zero padding, and the RHS (|b_i|; 0 in the objective row).
     const int wr = ldw - nA;
@@ -1583,7 +1659,7 @@ struct Solver {
     xr = reinterpret_cast<double*>(smem + L.ext);
     yr = xr + round_up(m + 1, 4);
     rf = reinterpret_cast<float*>(yr + round_up(m + 1, 4));
-    gam = L.gam >= 0 ? reinterpret_cast<unsigned long long*>(smem + L.gam) : nullptr;
+    gam = L.gam >= 0 ? reinterpret_cast<uint2*>(smem + L.gam) : nullptr;
   }
 
   __device__ void run(const LpArgs& a, const ClassArgs& ca) {
