@@ -519,9 +519,11 @@ struct Solver {
   // are read from the tableau and copied into colx / rhsx on the way, the
   // first pass's barrier publishing them (single-CTA steepest-edge loop);
   // with zero_sl the tableau's slot is also cleared in rows 0..m-1, as the
-  // FP32 steepest-edge sweep expects.
+  // FP32 steepest-edge sweep expects.  With recip the ratios are formed with
+  // one reciprocal per row (the FP32 steepest-edge loops, which are not held
+  // to the oracle's pivot sequence; the Dantzig loops divide, as it does).
   __device__ Key ratio(const Geom& g, T* colx, T piv_tol, T feas_tol, bool harris, T& theta,
-                       int fuse_sl = -1, bool zero_sl = false) {
+                       int fuse_sl = -1, bool zero_sl = false, bool recip = false) {
     auto fetch = [&](int i, T& a, T& rh) {
       if (fuse_sl >= 0) {
         a = tab[(size_t)i * g.ldw + fuse_sl];
@@ -550,12 +552,25 @@ struct Solver {
       theta = key_theta(k, T(0));
       return k;
     }
+    // pass 1 also keeps every eligible row's ratio rh / a (0 when rh <= 0)
+    // in the other column buffer (free during the ratio test), so that pass
+    // 2 and theta reuse it
+    T* thx = colx == col0 ? col1 : col0;
     for (int i = threadIdx.x; i < g.m; i += blockDim.x) {
       T a, rh;
       fetch(i, a, rh);
       if (a > piv_tol) {
         const T rr = rh > T(0) ? rh : T(0);
-        const T th1 = (rr + feas_tol) / a;
+        T th1, th;
+        if (recip) {
+          const T ra = sdiv(T(1), a);
+          th1 = (rr + feas_tol) * ra;
+          th = rr * ra;
+        } else {
+          th1 = (rr + feas_tol) / a;
+          th = rr / a;
+        }
+        thx[i] = th;
         Key kk = ratio_key(th1, 0, i);
         if (key_less(kk, k)) k = kk;
       }
@@ -566,19 +581,13 @@ struct Solver {
     Key k2 = key_none();
     for (int i = threadIdx.x; i < g.m; i += blockDim.x) {
       const T a = colx[i];
-      if (a > piv_tol) {
-        const T rh = rhsx[i];
-        const T th = rh > T(0) ? rh / a : T(0);
-        if (th <= tmax) {
-          Key kk = big_key(a, basis[i], i);
-          if (key_less(kk, k2)) k2 = kk;
-        }
+      if (a > piv_tol && thx[i] <= tmax) {
+        Key kk = big_key(a, basis[i], i);
+        if (key_less(kk, k2)) k2 = kk;
       }
     }
     k2 = block_min<kW1>(k2, redH);
-    const int r = (int)k2.w3;
-    const T a = colx[r], rh = rhsx[r];
-    theta = rh > T(0) ? rh / a : T(0);
+    theta = thx[(int)k2.w3];
     return k2;
   }
 
@@ -587,8 +596,10 @@ struct Solver {
   // row is updated with its slot s entry taken as 0 (the leaving variable's
   // reduced cost before the pivot), and the next column is priced; lv is the
   // leaving variable, now the label of slot s.
+  // recip: the pivot row times 1/pivot (the FP32 steepest-edge loop, not
+  // held to the oracle's pivot sequence) instead of divided by the pivot.
   __device__ Key pivot_rows(const Geom& g, int r, int s, int lv, const T* pcol, int c0,
-                            int lc, bool bland, T opt_tol, int price_cols) {
+                            int lc, bool bland, T opt_tol, int price_cols, bool recip = false) {
     const T piv = pcol[r];
     const T dq = pcol[g.m];
     const T rcp = sdiv(T(1), piv);
@@ -600,7 +611,7 @@ struct Solver {
     // one element per thread (the row is short: a few hundred entries), so
     // that each thread waits on one division, not a vector of them
     for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) {
-      const T p = lj == sl ? rcp : sdiv(prow[lj], piv);
+      const T p = lj == sl ? rcp : (recip ? prow[lj] * rcp : sdiv(prow[lj], piv));
       prow[lj] = p;
       T d = drow[lj];
       if (dq != T(0)) {
@@ -881,8 +892,11 @@ struct Solver {
                          int& cur, int period = 0) {
     const T opt_tol = (T)a.opt_tol, piv_tol = (T)a.piv_tol, feas_tol = (T)a.feas_tol;
     const T deg_tol = (T)a.deg_tol;
-    // FP32 on one CTA: the sweep with the entering slot and row r prepared
+    // FP32 on one CTA: the sweep with the entering slot and row r prepared;
+    // FP32: ratios and the pivot row with reciprocals (on any cluster size, so
+    // that a split tableau gives the same bits)
     constexpr bool kPre = sizeof(T) == 4 && !CLUSTER;
+    constexpr bool kRecip = sizeof(T) == 4;
     norms_full(g, lc);
     for (;;) {
       Key kq = price_se(g, c0, lc, bland, opt_tol, price_cols, w);
@@ -897,7 +911,7 @@ struct Solver {
         // reads are done: its argmin ended with a barrier); the column is
         // extracted inside the ratio test's first pass (FP32: and cleared)
         for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = make_uint2(0u, 0u);
-        kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta, s, kPre);
+        kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta, s, kPre, kRecip);
       } else {
         const int owner = s / g.cw;
         if (owner == rank) extract(g, s, c0, colbuf(cur));
@@ -914,7 +928,8 @@ struct Solver {
         __syncthreads();
         for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = make_uint2(0u, 0u);
         // ratio test: every CTA holds the column, so each computes it
-        kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta);
+        kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta, -1, false,
+                   kRecip);
       }
       const int r = kr.w2 == ~0u ? -1 : (int)kr.w3;
       if (r < 0) {
@@ -938,7 +953,7 @@ struct Solver {
         T* fcol = colbuf(cur ^ 1);
         for (int i = threadIdx.x; i < g.m; i += blockDim.x) fcol[i] = i == r ? T(0) : pcol[i];
       }
-      pivot_rows(g, r, s, lv, pcol, c0, lc, false, T(0), 0);
+      pivot_rows(g, r, s, lv, pcol, c0, lc, false, T(0), 0, kRecip);
       relabel(r, s, q, lv);
       if (kPre)
         update_body_se32(g, r, colbuf(cur ^ 1), lc);
