@@ -662,6 +662,7 @@ struct Solver {
   // by the ratio test and fcol is the pivot column with row r's entry 0, so
   // every row is t + f * p, stored where f != 0.  A row with f == 0 computes
   // t back (p is finite), so the norms take every computed row as it is.
+  // The RHS replica is not extracted: the next ratio test reads the tableau.
   __device__ void update_body_se32(const Geom& g, int r, const T* fcol, int lc) {
     update_rows<true, true>(tab, rhsx, rank, g.m, g.ldw, g.nl, g.cw, r, -1, fcol, -1, -1, 0,
                             nullptr, gam, lc);
@@ -702,10 +703,10 @@ struct Solver {
     // branch, only predicated stores.
     auto row = [&](const int i, const T f, const VT t) {
       if constexpr (PRE) {
-        // slot s and row r were prepared by the caller
+        // slot s and row r were prepared by the caller; the RHS is not
+        // extracted (that loop's ratio test reads it from the tableau)
         const VT tn = v_fma(f, p, t);
         if (f != T(0)) *reinterpret_cast<VT*>(tb + (size_t)i * ldw + lane * V) = tn;
-        if (has_rhs) rhsx[i] = vget<VT, T>(tn, 0);
         sq = v_sq(tn, sq);
         return;
       }
