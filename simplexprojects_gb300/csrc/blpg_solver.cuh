@@ -327,26 +327,27 @@ __device__ __forceinline__ float mag_f32(double x) {
   const unsigned bits = ((unsigned)e << 23) | ((hi & 0xFFFFFu) << 3);
   return e <= 0 ? 0.f : (e >= 255 ? 3.4e38f : __uint_as_float(bits));
 }
-// FP64 -> FP32 rounded to nearest even, built with integer operations (the
-// FP64-to-FP32 conversion instruction runs at GB300's low FP64 rate).  A
+// FP64 -> FP32 for the tableau, built with integer operations and selects
+// (the FP64-to-FP32 conversion instruction runs at GB300's low FP64 rate, and
+// per-element branches would diverge on every mix of zeros and nonzeros).  A
 // funnel shift of the two halves left by 3 puts the low 8 bits of the FP64
 // exponent e and the top 23 fraction bits where FP32 keeps its exponent and
-// fraction; for e in [897, 1149] the FP32 exponent e - 896 equals those 8
+// fraction; for e in [897, 1150] the FP32 exponent e - 896 equals those 8
 // bits with the top one flipped.  The 29 dropped bits round up above one half
 // and at one half when the kept bits are odd: their sum with 2^28 - 1 plus
 // the kept lowest bit carries out of bit 29 exactly then (a carry into the
-// exponent is the correctly rounded result).  FP64 zeros and subnormals (far
-// below FP32's smallest subnormal) become zeros of their sign; only results
-// below FP32's normal range and values near or above its maximum take the
-// conversion instruction.
+// exponent is the correctly rounded result, up to infinity).  Larger values
+// give infinity (NaN stays NaN); values below FP32's normal range (below
+// 1.2e-38, where FP32 would have subnormals) give zero of their sign.
 __device__ __forceinline__ float f64_to_f32_rn(double x) {
   const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-  const unsigned e = (hi >> 20) & 0x7FFu;
+  const unsigned e = (hi >> 20) & 0x7FFu, sign = hi & 0x80000000u;
   unsigned bits = (__funnelshift_l(lo, hi, 3) & 0x7FFFFFFFu) ^ 0x40000000u;
   bits += ((lo & 0x1FFFFFFFu) + 0x0FFFFFFFu + (bits & 1u)) >> 29;
-  if (e - 897u < 253u) return __uint_as_float(bits | (hi & 0x80000000u));
-  if (e == 0u) return __uint_as_float(hi & 0x80000000u);
-  return (float)x;
+  const bool nan = e == 0x7FFu && ((hi & 0xFFFFFu) | lo) != 0u;
+  const unsigned big = nan ? 0x7FC00000u : 0x7F800000u;
+  const unsigned out = e - 897u < 254u ? bits : (e >= 897u ? big : 0u);
+  return __uint_as_float(sign | out);
 }
 __device__ __forceinline__ float to_tab(double x, float) { return f64_to_f32_rn(x); }
 __device__ __forceinline__ double to_tab(double x, double) { return x; }
