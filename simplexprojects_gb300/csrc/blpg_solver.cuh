@@ -1476,16 +1476,21 @@ struct Solver {
         }
         badp = badp || xr[i] < -a.ptol;
       }
-      if (tid == 0) {
+      // z = c_B^T x_B: warp 0, lane-strided partial sums over the structural
+      // basics combined by a butterfly (a fixed order)
+      if (warp == 0) {
         double z = 0.0;
-        for (int t = 0; t < ns; ++t) {
+        for (int t = lane; t < ns; t += 32) {
           const int i = slist[t];
           z = fma(c[basis[i]], xr[i], z);
         }
-        sh->z = z;
-        for (int o = 0; o < K; ++o) {
-          T* p = tab + (size_t)m * g.ldw + g.cw;
-          *(o == rank ? p : remote(p, o)) = (T)z;
+        for (int o = 16; o > 0; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
+        if (lane == 0) {
+          sh->z = z;
+          for (int o = 0; o < K; ++o) {
+            T* p = tab + (size_t)m * g.ldw + g.cw;
+            *(o == rank ? p : remote(p, o)) = (T)z;
+          }
         }
       }
       badd = __syncthreads_or(badd ? 1 : 0) != 0;
