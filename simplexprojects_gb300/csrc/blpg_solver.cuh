@@ -172,7 +172,7 @@ struct Layout {
     // FP32 tableau: FP64 x_B and duals of the refresh, FP32 residual copy
     const int ext_bytes = elem == 4 ? 2 * mp1 * 8 + mp1 * 4 : 0;
     off += ext_bytes;
-    // steepest edge: one 64-bit fixed-point norm per local column slot,
+    // steepest edge: two 32-bit fixed-point norm counters per local column slot,
     // sharing the refresh's region when it is large enough (the norms are
     // recomputed after every refresh)
     gam = -1;
