@@ -93,11 +93,13 @@ struct blpg_plan {
   std::vector<int32_t> m, n, na;
   std::vector<int64_t> offA, offb, offc, offx, offbasis;
   int64_t extA = 0, extb = 0, extc = 0, extx = 0, extbasis = 0, extw = 0;
+  int64_t minA = 0;  // smallest offset into A
   std::vector<blpg::ClassPlan> classes;
   std::vector<int32_t> order;
   // device arrays
   int32_t *d_m = nullptr, *d_n = nullptr, *d_order = nullptr, *d_tickets = nullptr;
   int64_t *d_off = nullptr;  // offA | offb | offc | offx | offbasis
+  float* d_A32 = nullptr;    // FP32 plans: A rounded to FP32, elements [minA, extA) filled
   cudaStream_t stream = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_fork = nullptr;
   std::vector<cudaStream_t> aux;      // one per class after the first
@@ -119,6 +121,7 @@ static void release(blpg_plan* p) {
   cudaFree(p->d_order);
   cudaFree(p->d_tickets);
   cudaFree(p->d_off);
+  cudaFree(p->d_A32);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
   if (p->ev_out) cudaEventDestroy(p->ev_out);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
@@ -362,11 +365,28 @@ static int launch_one(blpg_plan* p, size_t ci, const LpArgs& args, cudaStream_t 
 
 // Queue reset, then every class on its own stream (fork/join through
 // events, so a captured graph has one parallel branch per class).
+// A rounded to FP32 for FP32 tableau loads: elements [lo, hi) of A, the same
+// rounding as the in-kernel loader's (f64_to_f32_rn); a grid-stride pass at
+// HBM speed.
+__global__ void round_a32_kernel(const double* __restrict__ A, float* __restrict__ A32,
+                                 long long lo, long long hi) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x; e < hi; e += stride)
+    A32[e] = dev::f64_to_f32_rn(__ldg(A + e));
+}
+
 template <typename T>
 static int launch_classes(blpg_plan* p, const LpArgs& args, cudaStream_t s) {
   CK(cudaMemsetAsync(p->d_tickets, 0, sizeof(int32_t) * std::max<size_t>(1, p->classes.size()), s));
   const size_t nc = p->classes.size();
   if (nc == 0) return BLPG_OK;
+  if (args.A32) {  // A rounded to FP32 before any class loads a tableau
+    const long long span = p->extA - p->minA;
+    const int grid = (int)std::min<long long>((span + 255) / 256, 8LL * std::max(1, p->sm_count));
+    round_a32_kernel<<<grid, 256, 0, s>>>(args.A, const_cast<float*>(args.A32), p->minA,
+                                               p->extA);
+    CK(cudaGetLastError());
+  }
   CK(cudaEventRecord(p->ev_fork, s));
   for (size_t ci = 1; ci < nc; ++ci) CK(cudaStreamWaitEvent(p->aux[ci - 1], p->ev_fork, 0));
   for (size_t ci = 0; ci < nc; ++ci) {
@@ -489,6 +509,7 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
     pc += n;
     pbs += m;
     p->extA = std::max(p->extA, p->offA[k] + (int64_t)m * n);
+    p->minA = k == 0 ? p->offA[k] : std::min(p->minA, p->offA[k]);
     p->extb = std::max(p->extb, p->offb[k] + m);
     p->extc = std::max(p->extc, p->offc[k] + n);
     if (bt->b) {
@@ -543,6 +564,12 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
   CKF(cudaMalloc(&p->d_order, sizeof(int32_t) * Nn));
   CKF(cudaMalloc(&p->d_tickets, sizeof(int32_t) * nc));
   CKF(cudaMalloc(&p->d_off, sizeof(int64_t) * 6 * Nn));
+  if (p->precision == BLPG_FP32 && p->extA > 0) {
+    // FP32 tableaux load A from an FP32 copy rounded once per execute (one
+    // bandwidth-bound pass) instead of converting it in every CTA's loader
+    CKF(cudaMalloc(&p->d_A32, sizeof(float) * (size_t)p->extA));
+    p->launches += 1;
+  }
   if (N > 0) {
     std::vector<int64_t> off(6 * (size_t)N);
     std::copy(p->offA.begin(), p->offA.end(), off.begin());
@@ -598,6 +625,7 @@ extern "C" int32_t blpg_plan_execute_weighted(blpg_plan* p, const double* dA, co
   a.pricing = p->opt.pricing == BLPG_PRICE_STEEPEST ? 1 : 0;
   a.weight = price_weight;
   a.A = dA;
+  a.A32 = p->d_A32;
   a.b = db;
   a.c = dc;
   a.status = out->status;

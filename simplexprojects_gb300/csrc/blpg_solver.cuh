@@ -82,6 +82,7 @@ struct LpArgs {
   int32_t pricing;         // 0: Dantzig, 1: steepest edge (exact column norms)
   const float* weight;     // nullable: steepest-edge score weight per variable (n + m per LP)
   const int64_t* offw;     // offsets of `weight`
+  const float* A32;        // nullable: A rounded to FP32 (offsets of A), read by FP32 tableau loads
 };
 
 // Bits of the per-LP info output.
@@ -1552,6 +1553,47 @@ struct Solver {
     }
   }
 
+  // The same block from A already rounded to FP32 (A32, same offsets as A):
+  // rows 0..m-1 are plain copies (half the bytes of the FP64 rows, nothing
+  // to convert); row m (-c in a single-phase LP, 0 before phase I) is
+  // converted separately, so that no conversion sits in the row loop.
+  static __device__ __noinline__ void load_block32(float* __restrict__ const tb,
+                                                   const float* __restrict__ const Ac,
+                                                   const double* __restrict__ const cc,
+                                                   const int* __restrict__ const flags,
+                                                   const int m, const int n, const int nA,
+                                                   const int ldw, const int na) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    constexpr int kR = 2, kQ = 8;
+    for (int i0 = warp * kR; i0 < m; i0 += nw * kR) {
+      for (int j0 = 0; j0 < nA; j0 += 32 * kQ) {
+        float v[kR][kQ];
+#pragma unroll
+        for (int r = 0; r < kR; ++r) {
+          const int i = min(i0 + r, m - 1);  // a row past m - 1 is loaded, not stored
+#pragma unroll
+          for (int q = 0; q < kQ; ++q) {
+            const int j = j0 + q * 32 + lane;
+            v[r][q] = j < nA ? __ldg(Ac + (size_t)i * n + j) : 0.f;
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < kR; ++r) {
+          const int i = i0 + r;
+          if (i >= m) continue;
+          const bool neg = na > 0 && flags[i] >= 0;  // a negated constraint row
+#pragma unroll
+          for (int q = 0; q < kQ; ++q) {
+            const int j = j0 + q * 32 + lane;
+            if (j < nA) tb[(size_t)i * ldw + j] = neg ? -v[r][q] : v[r][q];
+          }
+        }
+      }
+    }
+    for (int j = threadIdx.x; j < nA; j += blockDim.x)
+      tb[(size_t)m * ldw + j] = na == 0 ? -f64_to_f32_rn(__ldg(cc + j)) : 0.f;
+  }
+
   // FP64 tableau: the structural block copied straight from rows of A (and
   // c for row m of a single-phase LP) by asynchronous 8-byte global-to-shared
   // copies, which need no registers, then the rows to negate negated in place.
@@ -1589,7 +1631,7 @@ struct Solver {
   // basic there and its slack takes column slot n + a); structural j sits in
   // slot j.  Coalesced along rows of A.
   __device__ void load(const Geom& g, int c0, int lc, const double* A, const double* b,
-                       const double* c) {
+                       const double* c, const float* A32 = nullptr) {
     const int tid = threadIdx.x, nt = blockDim.x;
     const int m = g.m, n = g.n, na = g.na;
     const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
@@ -1647,6 +1689,8 @@ struct Solver {
     const int nA = max(0, min(n - c0, lc));
     if constexpr (sizeof(T) == 8)
       load_rows_async(g, c0, nA, A, c);
+    else if (A32)
+      load_block32(reinterpret_cast<float*>(tab), A32 + c0, c + c0, flags, m, n, nA, ldw, na);
     else
       load_block(tab, A + c0, c + c0, flags, m, n, nA, ldw, na);
     // The rest of every row: slack slots of negated rows (-1 in their own
@@ -1700,6 +1744,7 @@ struct Solver {
       const int lp = ca.order[t];
       const int m = a.m[lp], n = a.n[lp];
       const double* A = a.A + a.offA[lp];
+      const float* A32 = a.A32 ? a.A32 + a.offA[lp] : nullptr;
       const double* b = a.b + a.offb[lp];
       const double* c = a.c + a.offc[lp];
       // two-phase when any b_i < 0 (the reference's rem list, simplex.cu:574-583)
@@ -1723,7 +1768,7 @@ struct Solver {
       place(L, m);
       const int c0 = rank * g.cw;
       const int lc = max(0, min(g.cw, g.Wc - c0));
-      load(g, c0, lc, A, b, c);
+      load(g, c0, lc, A, b, c, A32);
       int pivots = 0, degen = 0, cur = 0, st, info = 0;
       const float* w = a.weight ? a.weight + a.offw[lp] : nullptr;
       bool bland = false;
@@ -1762,7 +1807,7 @@ struct Solver {
           if (attempt > 0) {
             info |= kInfoFallback;
             if (CLUSTER) csync();
-            load(g, c0, lc, A, b, c);
+            load(g, c0, lc, A, b, c, A32);
             piv_fresh = -1;
             bland = false;
             degen = 0;
@@ -1805,7 +1850,7 @@ struct Solver {
               // infeasible both ways (or dual simplex stuck): cold solve
               info |= kInfoFallback;
               if (CLUSTER) csync();
-              load(g, c0, lc, A, b, c);
+              load(g, c0, lc, A, b, c, A32);
               piv_fresh = -1;
               bland = false;
               degen = 0;
