@@ -193,9 +193,10 @@ int32_t blpg_solve_batch(const blpg_batch* batch, const blpg_options* opt,
 /* Plans: the size classes, work queues, device scratch and CUDA graph for
  * one batch shape, built once and replayed.  blpg_plan_create reads only the
  * shapes (count, m, n, offsets) of a HOST batch; A, b, c may be null.  An
- * FP32 plan also holds an FP32 copy of A (4 bytes per element up to the end
- * of the last LP's A), rounded from the executed A at the start of every
- * execute. */
+ * FP32 plan whose LPs share A (each element of A read by two LPs or more on
+ * average, e.g. one A for the whole batch) also holds an FP32 copy of A (4
+ * bytes per element up to the end of the last LP's A), rounded from the
+ * executed A at the start of every execute. */
 typedef struct blpg_plan blpg_plan;
 
 int32_t blpg_plan_create(const blpg_batch* host_shapes, const blpg_options* opt,

@@ -564,9 +564,14 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
   CKF(cudaMalloc(&p->d_order, sizeof(int32_t) * Nn));
   CKF(cudaMalloc(&p->d_tickets, sizeof(int32_t) * nc));
   CKF(cudaMalloc(&p->d_off, sizeof(int64_t) * 6 * Nn));
-  if (p->precision == BLPG_FP32 && p->extA > 0) {
-    // FP32 tableaux load A from an FP32 copy rounded once per execute (one
-    // bandwidth-bound pass) instead of converting it in every CTA's loader
+  // FP32 tableaux load A from an FP32 copy rounded once per execute (one
+  // bandwidth-bound pass) when LPs share A: every element of A's extent read
+  // by two LPs or more on average.  With an A per LP the copy would be an
+  // extra serial pass over all of A, and the loaders convert instead (their
+  // conversion overlaps other CTAs' pivots).
+  int64_t readA = 0;
+  for (int k = 0; k < N; ++k) readA += (int64_t)p->m[k] * p->n[k];
+  if (p->precision == BLPG_FP32 && p->extA > p->minA && readA >= 2 * (p->extA - p->minA)) {
     CKF(cudaMalloc(&p->d_A32, sizeof(float) * (size_t)p->extA));
     p->launches += 1;
   }
