@@ -521,7 +521,8 @@ struct Solver {
   // are read from the tableau and copied into colx / rhsx on the way, the
   // first pass's barrier publishing them (single-CTA steepest-edge loop);
   // with zero_sl the tableau's slot is also cleared in rows 0..m-1, as the
-  // FP32 steepest-edge sweep expects.  With recip the ratios are formed with
+  // FP32 steepest-edge sweep expects, and the RHS is not copied into rhsx
+  // (that loop reads it from the tableau).  With recip the ratios are formed with
   // one reciprocal per row (the FP32 steepest-edge loops, which are not held
   // to the oracle's pivot sequence; the Dantzig loops divide, as it does).
   __device__ Key ratio(const Geom& g, T* colx, T piv_tol, T feas_tol, bool harris, T& theta,
@@ -531,8 +532,10 @@ struct Solver {
         a = tab[(size_t)i * g.ldw + fuse_sl];
         rh = tab[(size_t)i * g.ldw + g.cw];
         colx[i] = a;
-        rhsx[i] = rh;
-        if (zero_sl) tab[(size_t)i * g.ldw + fuse_sl] = T(0);
+        if (zero_sl)
+          tab[(size_t)i * g.ldw + fuse_sl] = T(0);
+        else
+          rhsx[i] = rh;
       } else {
         a = colx[i];
         rh = rhsx[i];
@@ -554,10 +557,12 @@ struct Solver {
       theta = key_theta(k, T(0));
       return k;
     }
-    // pass 1 also keeps every eligible row's ratio rh / a (0 when rh <= 0)
-    // in the other column buffer (free during the ratio test), so that pass
-    // 2 and theta reuse it
-    T* thx = colx == col0 ? col1 : col0;
+    // pass 1 also keeps every eligible row's ratio rh / a (0 when rh <= 0),
+    // so that pass 2 and theta reuse it: in the other column buffer, or with
+    // zero_sl in rhsx (that loop writes its next multipliers into the other
+    // column buffer right after this returns, with no barrier between, and
+    // does not read rhsx)
+    T* thx = zero_sl ? rhsx : (colx == col0 ? col1 : col0);
     for (int i = threadIdx.x; i < g.m; i += blockDim.x) {
       T a, rh;
       fetch(i, a, rh);

@@ -104,3 +104,18 @@ def test_weights_need_steepest(built):
     w = np.ones(int((batch.n + batch.m).sum()), np.float32)
     with pytest.raises(sp.BlpgError):
         sp.solve(batch, "fp64", weight=w)
+
+
+@pytest.mark.parametrize("kind,count", [(1, 512), (2, 16), (3, 256)])
+def test_fp32_steepest_repeatable(built, kind, count):
+    """Repeated FP32 steepest-edge solves give the same bits: every value a
+    pivot's threads share (ratios, multipliers, norms) is published by a
+    barrier before it is overwritten."""
+    batch = sp.generate(kind, count, seed=sp.DEFAULT_SEED + 13 * kind)
+    a = sp.solve(batch, "fp32", pricing="steepest", want_x=True)
+    for _ in range(3):
+        b = sp.solve(batch, "fp32", pricing="steepest", want_x=True)
+        assert np.array_equal(a.status, b.status)
+        assert np.array_equal(a.pivots, b.pivots)
+        assert np.array_equal(a.objective, b.objective)
+        assert np.array_equal(a.x, b.x)
