@@ -215,3 +215,37 @@ def test_fp32_solutions_are_feasible(built, kind, period):
         scale = max(1.0, float(np.abs(b).max()), float(np.abs(xk).max()))
         assert (A @ xk - b).max() <= 1e-7 * scale, (k, g.status[k])
         assert xk.min() >= -1e-7 * scale, (k, g.status[k])
+
+
+def _shared_A(kind, count):
+    """A batch whose LPs share A: workload 3's families, or workload 0 in the
+    reference's batch mode (every LP on LP 0's A)."""
+    if kind == 3:
+        return sp.generate(3, count, seed=80, share_family_A=True)
+    g = sp.generate(0, count, seed=77)
+    m, n = int(g.m[0]), int(g.n[0])
+    assert (g.m == m).all() and (g.n == n).all()
+    return sp.LPBatch(g.m, g.n, g.A[:m * n].copy(), g.b, g.c,
+                      off_A=np.zeros(count, np.int64), off_b=g.off_b, off_c=g.off_c)
+
+
+@pytest.mark.parametrize("kind,count", [(0, 256), (3, 256)])
+def test_fp32_shared_A_copy_matches_private_A(built, kind, count):
+    """LPs that share A (each element read by two LPs or more) are loaded from
+    the plan's FP32 copy of A; the same LPs with a private copy of A each are
+    converted by the loaders.  Both give the same FP32 tableau, hence the same
+    bits."""
+    shared = _shared_A(kind, count)
+    oA, _, _ = shared.offsets()
+    reads = int((shared.m.astype(np.int64) * shared.n).sum())
+    assert reads >= 2 * len(shared.A)  # the plan makes the copy
+    parts = [shared.A[oA[k]:oA[k] + int(shared.m[k]) * int(shared.n[k])] for k in range(count)]
+    private = sp.LPBatch(shared.m, shared.n, np.concatenate(parts), shared.b, shared.c,
+                         off_b=shared.off_b, off_c=shared.off_c)
+    for pricing in ("dantzig", "steepest"):
+        a = sp.solve(shared, "fp32", pricing=pricing, want_x=True)
+        b = sp.solve(private, "fp32", pricing=pricing, want_x=True)
+        assert np.array_equal(a.status, b.status)
+        assert np.array_equal(a.pivots, b.pivots)
+        assert np.array_equal(a.objective, b.objective)
+        assert np.array_equal(a.x, b.x)
