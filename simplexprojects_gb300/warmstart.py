@@ -360,9 +360,11 @@ class LearnedSolver:
         """End to end from host arrays (same shapes and offsets as at
         construction): upload A, b, c, predict, solve, download results."""
         torch = self.torch
-        self.db.A.copy_(torch.from_numpy(batch.A), non_blocking=False)
-        self.db.b.copy_(torch.from_numpy(batch.b))
-        self.db.c.copy_(torch.from_numpy(batch.c))
+        # asynchronous when the host arrays are pinned (stream-ordered before
+        # the solve; result() synchronises)
+        self.db.A.copy_(torch.from_numpy(batch.A), non_blocking=True)
+        self.db.b.copy_(torch.from_numpy(batch.b), non_blocking=True)
+        self.db.c.copy_(torch.from_numpy(batch.c), non_blocking=True)
         self.d["fam"].copy_(torch.from_numpy(batch.family.astype(np.int32)))
         self.run()
         return self.db.result()
