@@ -738,15 +738,19 @@ struct Workspace {
   void* buf = nullptr;
   size_t cap = 0;
   blpg_plan* plan = nullptr;
-  std::vector<int32_t> key_shapes;
+  std::vector<int32_t> key_shapes;  // m, n per LP
+  std::vector<int32_t> key_negs;    // count of b_i < 0 per LP
   std::vector<int64_t> key_offs;
   blpg_options key_opt{};
 };
 static Workspace g_ws;
 
-static bool plan_matches(const Workspace& w, const blpg_batch* bt, const blpg_options& o,
-                         const std::vector<int32_t>& shapes,
-                         const std::vector<int64_t>& offs) {
+// The cached plan fits the batch's shapes, offsets and options (its
+// negative-b counts are checked separately): its workspace layout then fits
+// too, since that depends only on shapes and offsets.
+static bool plan_layout_matches(const Workspace& w, const blpg_batch* bt, const blpg_options& o,
+                                const std::vector<int32_t>& shapes,
+                                const std::vector<int64_t>& offs) {
   blpg_options a = w.key_opt, b = o;
   a.basis_hint = nullptr;
   b.basis_hint = nullptr;
@@ -771,108 +775,128 @@ extern "C" int32_t blpg_solve_batch(const blpg_batch* bt, const blpg_options* op
   else
     blpg_options_init(&opt);
   const int N = bt->count;
-  // plan cache key: shapes, offsets, negative-b counts, options
-  std::vector<int32_t> shapes(3 * (size_t)N);
-  std::vector<int64_t> offs;
-  int64_t pb = 0;
+  // plan cache key: shapes, offsets and options, then the negative-b counts
+  std::vector<int32_t> shapes(2 * (size_t)N);
   for (int k = 0; k < N; ++k) {
-    shapes[3 * k] = bt->m[k];
-    shapes[3 * k + 1] = bt->n[k];
-    const int64_t ob = bt->off_b ? bt->off_b[k] : pb;
-    int neg = 0;
-    if (bt->m[k] > 0)
-      for (int i = 0; i < bt->m[k]; ++i) neg += bt->b[ob + i] < 0.0 ? 1 : 0;
-    shapes[3 * k + 2] = neg;
-    pb += bt->m[k] > 0 ? bt->m[k] : 0;
+    shapes[2 * k] = bt->m[k];
+    shapes[2 * k + 1] = bt->n[k];
   }
+  std::vector<int64_t> offs;
   if (bt->off_A) offs.insert(offs.end(), bt->off_A, bt->off_A + N);
   if (bt->off_b) offs.insert(offs.end(), bt->off_b, bt->off_b + N);
   if (bt->off_c) offs.insert(offs.end(), bt->off_c, bt->off_c + N);
   offs.push_back(bt->off_A ? 1 : 0);
   offs.push_back(bt->off_b ? 2 : 0);
   offs.push_back(bt->off_c ? 4 : 0);
+  auto count_negs = [&]() {
+    std::vector<int32_t> negs((size_t)N);
+    int64_t pb = 0;
+    for (int k = 0; k < N; ++k) {
+      const int64_t ob = bt->off_b ? bt->off_b[k] : pb;
+      int neg = 0;
+      for (int i = 0; i < bt->m[k]; ++i) neg += bt->b[ob + i] < 0.0 ? 1 : 0;
+      negs[k] = neg;
+      pb += bt->m[k] > 0 ? bt->m[k] : 0;
+    }
+    return negs;
+  };
 
   std::lock_guard<std::mutex> lk(g_ws.mu);
   int rc;
-  if (!plan_matches(g_ws, bt, opt, shapes, offs)) {
-    if (g_ws.plan) {
-      blpg_plan_destroy(g_ws.plan);
-      g_ws.plan = nullptr;
-    }
-    if ((rc = blpg_plan_create(bt, &opt, &g_ws.plan))) return rc;
-    g_ws.key_shapes = shapes;
-    g_ws.key_offs = offs;
-    g_ws.key_opt = opt;
-  }
-  blpg_plan* p = g_ws.plan;
-  // workspace: A | b | c | status | obj | x | pivots | basis (256-byte aligned)
-  auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-  const size_t sA = al(sizeof(double) * p->extA), sb = al(sizeof(double) * p->extb),
-               sc = al(sizeof(double) * p->extc), sst = al(sizeof(int32_t) * N),
-               sob = al(sizeof(double) * N), sx = al(sizeof(double) * p->extx),
-               spv = al(sizeof(int32_t) * N), sbs = al(sizeof(int32_t) * p->extbasis);
   const bool hint = opt.basis_hint != nullptr;
   const bool wt = opt.price_weight != nullptr;
   if (wt && opt.pricing != BLPG_PRICE_STEEPEST)
     return fail(BLPG_EINVAL, "blpg_solve_batch: pricing weights need steepest-edge pricing");
-  const size_t sw = al(sizeof(float) * p->extw);
-  const size_t need = sA + sb + sc + sst + sob + (out->x ? sx : 0) +
-                      (out->pivots ? spv : 0) + (out->basis ? sbs : 0) +
-                      (out->info ? spv : 0) + (hint ? sbs : 0) + (wt ? sw : 0);
-  if (g_ws.cap < need || g_ws.device != p->device) {
-    if (g_ws.buf) cudaFree(g_ws.buf);
-    g_ws.buf = nullptr;
-    g_ws.cap = 0;
-    CK(cudaMalloc(&g_ws.buf, need));
-    g_ws.cap = need;
-    g_ws.device = p->device;
+  // workspace: A | b | c | status | obj | x | pivots | info | hint | weights
+  // (256-byte aligned); its layout depends only on shapes and offsets
+  auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  struct Slots {
+    double *A, *b, *c;
+    blpg_result res;
+    int32_t* hint;
+    float* w;
+  };
+  auto carve = [&](blpg_plan* p, Slots& sl) -> int {
+    const size_t sA = al(sizeof(double) * p->extA), sb = al(sizeof(double) * p->extb),
+                 sc = al(sizeof(double) * p->extc), sst = al(sizeof(int32_t) * N),
+                 sob = al(sizeof(double) * N), sx = al(sizeof(double) * p->extx),
+                 spv = al(sizeof(int32_t) * N), sbs = al(sizeof(int32_t) * p->extbasis),
+                 sw = al(sizeof(float) * p->extw);
+    const size_t need = sA + sb + sc + sst + sob + (out->x ? sx : 0) +
+                        (out->pivots ? spv : 0) + (out->basis ? sbs : 0) +
+                        (out->info ? spv : 0) + (hint ? sbs : 0) + (wt ? sw : 0);
+    if (g_ws.cap < need || g_ws.device != p->device) {
+      if (g_ws.buf) cudaFree(g_ws.buf);
+      g_ws.buf = nullptr;
+      g_ws.cap = 0;
+      CK(cudaMalloc(&g_ws.buf, need));
+      g_ws.cap = need;
+      g_ws.device = p->device;
+    }
+    char* o = (char*)g_ws.buf;
+    sl = Slots{};
+    sl.A = (double*)o;
+    o += sA;
+    sl.b = (double*)o;
+    o += sb;
+    sl.c = (double*)o;
+    o += sc;
+    sl.res.status = (int32_t*)o;
+    o += sst;
+    sl.res.objective = (double*)o;
+    o += sob;
+    if (out->x) sl.res.x = (double*)o, o += sx;
+    if (out->pivots) sl.res.pivots = (int32_t*)o, o += spv;
+    if (out->basis) sl.res.basis = (int32_t*)o, o += sbs;
+    if (out->info) sl.res.info = (int32_t*)o, o += spv;
+    if (hint) sl.hint = (int32_t*)o, o += sbs;
+    if (wt) sl.w = (float*)o, o += sw;
+    return BLPG_OK;
+  };
+  auto upload = [&](blpg_plan* p, const Slots& sl) -> int {
+    cudaStream_t s = p->stream;
+    if (hint)
+      CK(cudaMemcpyAsync(sl.hint, opt.basis_hint, sizeof(int32_t) * p->extbasis,
+                         cudaMemcpyHostToDevice, s));
+    if (wt)
+      CK(cudaMemcpyAsync(sl.w, opt.price_weight, sizeof(float) * p->extw,
+                         cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sl.A, bt->A, sizeof(double) * p->extA, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sl.b, bt->b, sizeof(double) * p->extb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sl.c, bt->c, sizeof(double) * p->extc, cudaMemcpyHostToDevice, s));
+    return BLPG_OK;
+  };
+  Slots sl{};
+  bool uploaded = false;
+  if (plan_layout_matches(g_ws, bt, opt, shapes, offs)) {
+    // the cached plan's layout fits: the uploads start now and the host
+    // counts negative b's while they run
+    if ((rc = carve(g_ws.plan, sl)) || (rc = upload(g_ws.plan, sl))) return rc;
+    uploaded = true;
   }
-  char* base = (char*)g_ws.buf;
-  double* dA = (double*)base;
-  double* db = (double*)(base + sA);
-  double* dc = (double*)(base + sA + sb);
-  char* o = base + sA + sb + sc;
-  blpg_result dres{};
-  dres.status = (int32_t*)o;
-  o += sst;
-  dres.objective = (double*)o;
-  o += sob;
-  if (out->x) {
-    dres.x = (double*)o;
-    o += sx;
+  std::vector<int32_t> negs = count_negs();
+  if (!uploaded || negs != g_ws.key_negs) {
+    if (g_ws.plan) {
+      blpg_plan_destroy(g_ws.plan);  // synchronises its stream (the uploads land)
+      g_ws.plan = nullptr;
+    }
+    if ((rc = blpg_plan_create(bt, &opt, &g_ws.plan))) return rc;
+    g_ws.key_shapes = shapes;
+    g_ws.key_negs = negs;
+    g_ws.key_offs = offs;
+    g_ws.key_opt = opt;
+    if (!uploaded) {
+      if ((rc = carve(g_ws.plan, sl)) || (rc = upload(g_ws.plan, sl))) return rc;
+    }
   }
-  if (out->pivots) {
-    dres.pivots = (int32_t*)o;
-    o += spv;
-  }
-  if (out->basis) {
-    dres.basis = (int32_t*)o;
-    o += sbs;
-  }
-  if (out->info) {
-    dres.info = (int32_t*)o;
-    o += spv;
-  }
-  int32_t* dhint = nullptr;
-  if (hint) {
-    dhint = (int32_t*)o;
-    o += sbs;
-  }
-  float* dw = nullptr;
-  if (wt) {
-    dw = (float*)o;
-    o += sw;
-  }
+  blpg_plan* p = g_ws.plan;
   cudaStream_t s = p->stream;
-  if (hint)
-    CK(cudaMemcpyAsync(dhint, opt.basis_hint, sizeof(int32_t) * p->extbasis,
-                       cudaMemcpyHostToDevice, s));
-  if (wt)
-    CK(cudaMemcpyAsync(dw, opt.price_weight, sizeof(float) * p->extw, cudaMemcpyHostToDevice,
-                       s));
-  CK(cudaMemcpyAsync(dA, bt->A, sizeof(double) * p->extA, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(db, bt->b, sizeof(double) * p->extb, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(dc, bt->c, sizeof(double) * p->extc, cudaMemcpyHostToDevice, s));
+  double* dA = sl.A;
+  double* db = sl.b;
+  double* dc = sl.c;
+  blpg_result& dres = sl.res;
+  int32_t* dhint = sl.hint;
+  float* dw = sl.w;
   if ((rc = blpg_plan_execute_weighted(p, dA, db, dc, dhint, dw, &dres, s))) return rc;
   CK(cudaMemcpyAsync(out->status, dres.status, sizeof(int32_t) * N, cudaMemcpyDeviceToHost,
                      s));
