@@ -748,8 +748,8 @@ struct Solver {
     for (; i0 < m; i0 += G)
       row(i0, pcol[i0], *reinterpret_cast<const VT*>(tb + (size_t)i0 * ldw + lane * V));
     if (SE) {
-      // columns visited in a rotated order, so that the 64-bit counters of
-      // one instruction fall in distinct banks (two wavefronts, not eight)
+      // columns visited in a rotated order, so that the counter pairs of one
+      // instruction fall in distinct banks (two wavefronts, not eight)
 #pragma unroll
       for (int e2 = 0; e2 < V; ++e2) {
         const int e = (e2 + (lane >> 2)) & (V - 1);
