@@ -249,3 +249,31 @@ def test_fp32_shared_A_copy_matches_private_A(built, kind, count):
         assert np.array_equal(a.pivots, b.pivots)
         assert np.array_equal(a.objective, b.objective)
         assert np.array_equal(a.x, b.x)
+
+
+def test_fp32_shared_A_copy_phase_one(built):
+    """Phase-I LPs (some b_i < 0: negated rows, a zero objective row until
+    phase II) loaded from the FP32 copy of a shared A give the bits of the
+    in-kernel conversion and the oracle's statuses.  A has mixed signs and
+    b = A x0 + slack for x0 >= 0, so every LP is feasible."""
+    base = _shared_A(0, 256)
+    m, n = int(base.m[0]), int(base.n[0])
+    rng = np.random.default_rng(5)
+    A = base.A.copy().reshape(m, n)
+    A[rng.random((m, n)) < 0.3] *= -1
+    x0 = rng.random((256, n)) * (rng.random((256, n)) < 0.3)
+    b = (x0 @ A.T + rng.random((256, m)) * 0.5).reshape(-1)
+    shared = sp.LPBatch(base.m, base.n, A.reshape(-1), b, base.c, off_A=base.off_A,
+                        off_c=base.off_c)
+    assert (b.reshape(256, m) < 0).any(1).sum() > 200  # most LPs need phase I
+    private = sp.LPBatch(base.m, base.n, np.tile(A.reshape(-1), 256), b, base.c,
+                         off_c=base.off_c)
+    c64 = ref.solve_batch(shared, "fp64")
+    for pricing in ("dantzig", "steepest"):
+        a = sp.solve(shared, "fp32", pricing=pricing, want_x=True)
+        p = sp.solve(private, "fp32", pricing=pricing, want_x=True)
+        assert np.array_equal(a.status, p.status)
+        assert np.array_equal(a.pivots, p.pivots)
+        assert np.array_equal(a.objective, p.objective)
+        assert np.array_equal(a.x, p.x)
+        assert np.array_equal(a.status, c64.status)
