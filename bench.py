@@ -29,6 +29,12 @@ on).  One step = one solve of the whole workload batch.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload 0..4]
                   [--precision fp64|fp32] [--impl blpg|reference]
+  python bench.py --profile-case N [--workload K] [--precision P] [--pricing R]
+               a small solve for ncu captures: N LPs of the workload (families
+               sharing A) solved twice on a device-resident plan (the second
+               launch is the capture target); prints the class plan, the
+               status histogram and the pivot total.  A few MB on the device,
+               so a full-metric capture of one solve launch ends in a minute.
 """
 from __future__ import annotations
 
@@ -165,7 +171,7 @@ def cpu_baseline(batch, precision: str, budget_s: float = 12.0):
     r = ref.solve_batch(sample, precision, threads=threads)
     dt = time.perf_counter() - t0
     return {"value": k2 / dt, "unit": "LPs/s", "cores": threads, "kind": "port",
-            "pivots_per_s": float(r.pivots.sum()) / dt,
+            "pivots_per_s": float(r.pivots.sum()) / dt, "ms": dt * 1e3, "lps": k2,
             "sample": f"first {k2} LPs of the workload, {precision} oracle, {dt:.1f}s"}
 
 
@@ -180,6 +186,9 @@ def run_reference(args, rank, world):
     print(json.dumps({
         "impl": "reference", "metric": "LPs/s", "value": v, "unit": "LPs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        # one step = one timed sample of the workload (a bounded CPU run)
+        "ms_per_step": statistics.median(x["ms"] for x in vals),
+        "step_ms_all": [x["ms"] for x in vals],
         "dtype": "f64" if args.precision == "fp64" else "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD_NAMES[args.workload], "precision": args.precision,
                    "lps": total},
@@ -355,6 +364,19 @@ def run_learned(args, rank, world, local, dist=None):
     print(json.dumps(out))
 
 
+def run_profile_case(args):
+    import simplexprojects_gb300 as sp
+    batch = sp.generate(args.workload, args.profile_case, seed=sp.DEFAULT_SEED,
+                        share_family_A=True)
+    db = sp.DeviceBatch(batch, args.precision, pricing=args.pricing)
+    for _ in range(2):
+        db.run()
+    r = db.result()
+    print("classes", db.plan.classes())
+    print("status", np.bincount(r.status).tolist(), "pivots", int(r.pivots.sum()))
+    db.plan.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -367,7 +389,11 @@ def main():
     ap.add_argument("--pricing", default="dantzig", choices=["dantzig", "steepest"],
                     help="pricing rule of workloads 0-2, 4 (3 runs every variant)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", type=int, default=0, metavar="N",
+                    help="small solve of N LPs for ncu captures (see the module docstring)")
     args = ap.parse_args()
+    if args.profile_case > 0:
+        return run_profile_case(args)
     args.warmup = max(3, args.warmup)
 
     rank = int(os.environ.get("RANK", 0))

@@ -270,6 +270,17 @@ int32_t blpg_solve_noalloc(int32_t count, int32_t max_m, int32_t max_n,
                            double* d_objective, double* d_x, int32_t* d_pivots,
                            void* stream);
 
+/* FP64 -> FP32 rounding of FP32 tableaux, over `count` device doubles into
+ * device floats, asynchronous on `stream`.  mode 0: the rounding the FP32
+ * tableau loaders and the FP32 copy of A use (IEEE round-to-nearest-even,
+ * built from integer operations; values below FP32's normal range, |x| <
+ * 2^-126, become zero of their sign instead of FP32 subnormals); mode 1:
+ * CUDA's __double2float_rn, for comparison.  No reference counterpart (the
+ * reference's FP32 kernel, CPLEXvsGLPK/SourceCode/src/simplex.cu, reads
+ * float input directly). */
+int32_t blpg_round_f32(const double* d_in, float* d_out, int64_t count, int32_t mode,
+                       void* stream);
+
 /* Roofline denominators of the pivot kernels, timed on `device` by synthetic
  * kernels: shared-memory bandwidth (GB/s, bytes read + written) and FP64 /
  * FP32 FMA throughput (TFLOP/s, 2 flops per FMA).  No reference counterpart

@@ -21,7 +21,8 @@ from typing import Optional
 
 import numpy as np
 
-DEFAULT_LIB = os.environ.get("BLPG_GLPK_LIB", "/root/reference/lib/libglpk.so.0.30.0")
+REFERENCE = os.environ.get("BLPG_REFERENCE", "/root/reference")
+DEFAULT_LIB = os.environ.get("BLPG_GLPK_LIB", os.path.join(REFERENCE, "lib", "libglpk.so.0.30.0"))
 
 GLP_MAX = 2
 GLP_LO, GLP_UP = 2, 3

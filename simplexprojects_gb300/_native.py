@@ -71,6 +71,7 @@ SIGNATURES = {
     "blpg_last_error": (C.c_char_p, []),
     "blpg_version": (C.c_char_p, []),
     "blpg_measure_peaks": (C.c_int32, [C.c_int32, f64p, f64p, f64p]),
+    "blpg_round_f32": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]),
     "blpg_solve_noalloc": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32] + [C.c_void_p] * 8
                            + [C.c_int32] + [C.c_void_p] * 5),
     "blpg_mlp_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,

@@ -375,6 +375,15 @@ __global__ void round_a32_kernel(const double* __restrict__ A, float* __restrict
     A32[e] = dev::f64_to_f32_rn(__ldg(A + e));
 }
 
+// The same rounding over a plain array, or CUDA's conversion instruction
+// (__double2float_rn) for comparison (blpg_round_f32).
+__global__ void round_f32_kernel(const double* __restrict__ in, float* __restrict__ out,
+                                 long long n, int cuda_rn) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride)
+    out[e] = cuda_rn ? __double2float_rn(in[e]) : dev::f64_to_f32_rn(in[e]);
+}
+
 template <typename T>
 static int launch_classes(blpg_plan* p, const LpArgs& args, cudaStream_t s) {
   CK(cudaMemsetAsync(p->d_tickets, 0, sizeof(int32_t) * std::max<size_t>(1, p->classes.size()), s));
@@ -687,6 +696,17 @@ extern "C" int32_t blpg_plan_execute_weighted(blpg_plan* p, const double* dA, co
   return BLPG_OK;
 }
 
+extern "C" int32_t blpg_round_f32(const double* d_in, float* d_out, int64_t count, int32_t mode,
+                                  void* stream) {
+  if (count < 0 || (count > 0 && (!d_in || !d_out)) || (mode != 0 && mode != 1))
+    return fail(BLPG_EINVAL, "blpg_round_f32: bad arguments");
+  if (count == 0) return BLPG_OK;
+  const int grid = (int)std::min<int64_t>((count + 255) / 256, 4096);
+  round_f32_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_in, d_out, (long long)count, mode);
+  CK(cudaGetLastError());
+  return BLPG_OK;
+}
+
 extern "C" int32_t blpg_plan_num_classes(const blpg_plan* p) {
   return p ? (int32_t)p->classes.size() : fail(BLPG_EINVAL, "null plan");
 }
@@ -748,15 +768,23 @@ static Workspace g_ws;
 // The cached plan fits the batch's shapes, offsets and options (its
 // negative-b counts are checked separately): its workspace layout then fits
 // too, since that depends only on shapes and offsets.
+// Options compared field by field (a memcmp would also compare the struct's
+// padding, which a caller's copy need not preserve); the per-call data
+// pointers basis_hint and price_weight are not part of the plan.
+static bool same_plan_options(const blpg_options& a, const blpg_options& b) {
+  return a.precision == b.precision && a.max_pivots == b.max_pivots &&
+         a.bland_after == b.bland_after && a.refactor_period == b.refactor_period &&
+         a.opt_tol == b.opt_tol && a.piv_tol == b.piv_tol && a.device == b.device &&
+         a.use_graph == b.use_graph && a.threads_per_cta == b.threads_per_cta &&
+         a.max_cluster == b.max_cluster && a.min_cluster == b.min_cluster &&
+         a.cta_smem_budget == b.cta_smem_budget && a.ratio_rule == b.ratio_rule &&
+         a.feas_tol == b.feas_tol && a.warm_mode == b.warm_mode && a.pricing == b.pricing;
+}
+
 static bool plan_layout_matches(const Workspace& w, const blpg_batch* bt, const blpg_options& o,
                                 const std::vector<int32_t>& shapes,
                                 const std::vector<int64_t>& offs) {
-  blpg_options a = w.key_opt, b = o;
-  a.basis_hint = nullptr;
-  b.basis_hint = nullptr;
-  a.price_weight = nullptr;
-  b.price_weight = nullptr;
-  return w.plan && std::memcmp(&a, &b, sizeof(a)) == 0 && w.key_shapes == shapes &&
+  return w.plan && same_plan_options(w.key_opt, o) && w.key_shapes == shapes &&
          w.key_offs == offs && w.plan->count == bt->count;
 }
 }  // namespace blpg

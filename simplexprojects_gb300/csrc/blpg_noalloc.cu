@@ -15,8 +15,10 @@
 //  - the scratch array (about 1 MiB) lives in every GPU that loads the
 //    library until the process exits;
 //  - the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress and sets the kernels' shared-memory attribute;
-//    make that first call before any stream capture;
+//    cudaGetSymbolAddress, reads the device's properties and sets the
+//    kernels' shared-memory attribute, under a lock (two host threads making
+//    their first call at once do the set-up once); make that first call
+//    before any stream capture;
 //  - every call reuses the same array: calls whose GPU work overlaps (two
 //    streams, or two host threads) race on it and must be serialised by the
 //    caller; each call resets the ticket and the order list before its solve;
@@ -26,8 +28,10 @@
 //  - no cudaMalloc, cudaFree, stream, event or graph is created.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 
 #include "blpg_internal.h"
 #include "blpg_solver.cuh"
@@ -48,11 +52,21 @@ __global__ void noalloc_reset(int32_t* scratch, int32_t count) {
 }
 
 // Per-device set-up, done once with that device current.  No heap use.
+// `ready` is published with release ordering after the other fields are
+// written, so a caller that reads it as true (acquire) sees them.  The
+// occupancy of the last launch shape per precision is cached as well, so a
+// repeated call makes no device queries.
 struct DevSetup {
+  std::atomic<bool> ready;
   int32_t* scratch;
-  bool ready;
+  int sm_count;
+  int max_smem;
+  std::mutex occ_mu;
+  int occ_key[2][3];  // [precision] (K, threads, smem) of the cached entry
+  int occ_val[2];     // CTAs per SM (K = 1) or clusters
 };
 static DevSetup g_setup[kMaxDevices];
+static std::mutex g_setup_mu;
 
 template <typename T>
 int32_t setup_attrs(int max_smem) {
@@ -68,13 +82,55 @@ int32_t setup_attrs(int max_smem) {
   return BLPG_OK;
 }
 
+// Occupancy of a launch shape (CTAs per SM for K = 1, else clusters),
+// answered from the per-device cache when the shape repeats.
+template <typename T>
+cudaError_t occupancy(DevSetup& st, int K, int nt, int smem, int* out) {
+  const int pi = sizeof(T) == 4 ? 1 : 0;
+  {
+    std::lock_guard<std::mutex> lk(st.occ_mu);
+    if (st.occ_key[pi][0] == K && st.occ_key[pi][1] == nt && st.occ_key[pi][2] == smem) {
+      *out = st.occ_val[pi];
+      return cudaSuccess;
+    }
+  }
+  using namespace blpg::dev;
+  cudaError_t e;
+  *out = 0;
+  if (K == 1) {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, solve_kernel<T, false>, nt, smem);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = K;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(K, 1, 1);
+    cfg.blockDim = dim3(nt, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    e = cudaOccupancyMaxActiveClusters(out, solve_kernel<T, true>, &cfg);
+  }
+  if (e == cudaSuccess && *out > 0) {
+    std::lock_guard<std::mutex> lk(st.occ_mu);
+    st.occ_key[pi][0] = K;
+    st.occ_key[pi][1] = nt;
+    st.occ_key[pi][2] = smem;
+    st.occ_val[pi] = *out;
+  }
+  return e;
+}
+
 template <typename T>
 int32_t run(int32_t count, int32_t max_m, int32_t max_n, const blpg::dev::LpArgs& a,
-            int32_t* scratch, const cudaDeviceProp& prop, cudaStream_t s) {
+            DevSetup& st, cudaStream_t s) {
   using blpg::fail;
   using namespace blpg::dev;
   constexpr int V = VecT<T>::V;
-  const int max_smem = (int)prop.sharedMemPerBlockOptin;
+  int32_t* scratch = st.scratch;
+  const int max_smem = st.max_smem;
   int K = 0, nt = 0, smem = 0;
   for (int k = 1; k <= 8; k *= 2) {
     Geom g(max_m, max_n, 0, k, V);
@@ -105,10 +161,10 @@ int32_t run(int32_t count, int32_t max_m, int32_t max_n, const blpg::dev::LpArgs
     return fail(BLPG_ECUDA, "blpg_solve_noalloc: reset launch: %s", cudaGetErrorString(e));
   if (K == 1) {
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, solve_kernel<T, false>, nt, smem);
+    e = occupancy<T>(st, 1, nt, smem, &per_sm);
     if (e != cudaSuccess || per_sm <= 0)
       return fail(BLPG_ECUDA, "blpg_solve_noalloc: occupancy query failed");
-    int grid = per_sm * prop.multiProcessorCount;
+    int grid = per_sm * st.sm_count;
     if (grid > count) grid = count;
     solve_kernel<T, false><<<grid, nt, smem, s>>>(a, ca);
   } else {
@@ -118,13 +174,12 @@ int32_t run(int32_t count, int32_t max_m, int32_t max_n, const blpg::dev::LpArgs
     at[0].val.clusterDim.x = K;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(K, 1, 1);
     cfg.blockDim = dim3(nt, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.attrs = at;
     cfg.numAttrs = 1;
     int clusters = 0;
-    e = cudaOccupancyMaxActiveClusters(&clusters, solve_kernel<T, true>, &cfg);
+    e = occupancy<T>(st, K, nt, smem, &clusters);
     if (e != cudaSuccess || clusters <= 0)
       return fail(BLPG_ECUDA, "blpg_solve_noalloc: cluster occupancy query failed");
     if (clusters > count) clusters = count;
@@ -165,23 +220,28 @@ extern "C" int32_t blpg_solve_noalloc(int32_t count, int32_t max_m, int32_t max_
   if (e != cudaSuccess) return fail(BLPG_ENODEV, "blpg_solve_noalloc: %s", cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices)
     return fail(BLPG_ENODEV, "blpg_solve_noalloc: device %d not supported", dev);
-  cudaDeviceProp prop;
-  e = cudaGetDeviceProperties(&prop, dev);
-  if (e != cudaSuccess || prop.major != 10 || prop.minor != 3)
-    return fail(BLPG_ENODEV, "blpg_solve_noalloc: device %d is not sm_103", dev);
   DevSetup& st = g_setup[dev];
-  if (!st.ready) {
-    void* ptr = nullptr;
-    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess || !ptr)
-      return fail(BLPG_ECUDA, "blpg_solve_noalloc: cudaGetSymbolAddress: %s",
-                  cudaGetErrorString(e));
-    const int max_smem = (int)prop.sharedMemPerBlockOptin;
-    int32_t rc = setup_attrs<double>(max_smem);
-    if (rc == BLPG_OK) rc = setup_attrs<float>(max_smem);
-    if (rc != BLPG_OK) return rc;
-    st.scratch = static_cast<int32_t*>(ptr);
-    st.ready = true;
+  if (!st.ready.load(std::memory_order_acquire)) {
+    std::lock_guard<std::mutex> lk(g_setup_mu);
+    if (!st.ready.load(std::memory_order_relaxed)) {
+      cudaDeviceProp prop;
+      e = cudaGetDeviceProperties(&prop, dev);
+      if (e != cudaSuccess || prop.major != 10 || prop.minor != 3)
+        return fail(BLPG_ENODEV, "blpg_solve_noalloc: device %d is not sm_103", dev);
+      void* ptr = nullptr;
+      e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess || !ptr)
+        return fail(BLPG_ECUDA, "blpg_solve_noalloc: cudaGetSymbolAddress: %s",
+                    cudaGetErrorString(e));
+      const int max_smem = (int)prop.sharedMemPerBlockOptin;
+      int32_t rc = setup_attrs<double>(max_smem);
+      if (rc == BLPG_OK) rc = setup_attrs<float>(max_smem);
+      if (rc != BLPG_OK) return rc;
+      st.scratch = static_cast<int32_t*>(ptr);
+      st.sm_count = prop.multiProcessorCount;
+      st.max_smem = max_smem;
+      st.ready.store(true, std::memory_order_release);
+    }
   }
   blpg::dev::LpArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -216,6 +276,6 @@ extern "C" int32_t blpg_solve_noalloc(int32_t count, int32_t max_m, int32_t max_
   a.warm_mode = 1;
   a.shift = 0.1;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return fp32 ? run<float>(count, max_m, max_n, a, st.scratch, prop, s)
-              : run<double>(count, max_m, max_n, a, st.scratch, prop, s);
+  return fp32 ? run<float>(count, max_m, max_n, a, st, s)
+              : run<double>(count, max_m, max_n, a, st, s);
 }

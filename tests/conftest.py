@@ -1,4 +1,5 @@
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -9,7 +10,9 @@ if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-REFERENCE = Path("/root/reference")
+# the reference checkout (x86 container only; absent on the GPU host)
+REFERENCE = Path(os.environ.get("BLPG_REFERENCE", "/root/reference"))
+NETLIB = GOLDEN / "netlib"
 
 
 def pytest_configure(config):

@@ -18,8 +18,15 @@ Fixtures:
                    GPU_Tester.cu:80-86) and the 8 Netlib LPs it ships
                    (benchmarks/*.txt, listed optima parseBenchmark.cpp:15-25),
                    solved by GLPK with exact verdicts
+  netlib/          byte-for-byte copies of those 8 Netlib LPs' A/B/C text
+                   files (public Netlib data in the reference's dense format,
+                   parseBenchmark.cpp:59-126), so that the GPU tests and the
+                   reference-compatible CLI can solve them where the
+                   reference checkout is absent
 
-Usage:  python tests/golden/make_golden.py [--quick]
+The reference checkout is read from $BLPG_REFERENCE (default /root/reference).
+
+Usage:  python tests/golden/make_golden.py [--quick] [--known-only] [--netlib-copy]
 """
 from __future__ import annotations
 
@@ -27,6 +34,8 @@ import argparse
 import hashlib
 import json
 import multiprocessing as mp
+import os
+import shutil
 import sys
 import time
 from pathlib import Path
@@ -40,7 +49,7 @@ sys.path.insert(0, str(ROOT))
 SEED = 20240611
 # (kind, first, count): LP indices of each workload's sample
 SAMPLES = {0: (0, 48), 1: (0, 40), 2: (0, 3), 3: (39_990, 6), 4: (0, 40)}
-REF = Path("/root/reference")
+REF = Path(os.environ.get("BLPG_REFERENCE", "/root/reference"))
 NETLIB = ["ADLITTLE", "AFIRO", "BLEND", "ISRAEL", "SC105", "SC205", "SC50A", "SC50B"]
 # listed optima of the minimisation files (parseBenchmark.cpp:15-25)
 NETLIB_LISTED = {
@@ -122,12 +131,32 @@ def _solve_one(args):
     return out
 
 
+def copy_netlib() -> list[str]:
+    """Copy the reference's Netlib A/B/C files into tests/golden/netlib/."""
+    dst = HERE / "netlib"
+    dst.mkdir(exist_ok=True)
+    copied = []
+    for nm in NETLIB:
+        srcs = [REF / "benchmarks" / f"{nm}_{s}.txt" for s in "ABC"]
+        if not all(p.exists() for p in srcs):
+            continue
+        for p in srcs:
+            shutil.copyfile(p, dst / p.name)
+        copied.append(nm)
+    return copied
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true", help="smaller samples (smoke the script)")
     ap.add_argument("--procs", type=int, default=8)
     ap.add_argument("--known-only", action="store_true", help="regenerate known.json only")
+    ap.add_argument("--netlib-copy", action="store_true",
+                    help="only copy the Netlib A/B/C files into tests/golden/netlib/")
     args = ap.parse_args()
+    print("netlib files copied:", copy_netlib())
+    if args.netlib_copy:
+        return
     import simplexprojects_gb300 as sp
     from oracle import glpk
     if not glpk.available():

@@ -8,7 +8,7 @@ import pytest
 
 import simplexprojects_gb300 as sp
 from oracle import ref, exact
-from conftest import REFERENCE
+from conftest import NETLIB, REFERENCE
 
 
 def _fp(batch):
@@ -86,12 +86,13 @@ def test_oracle_pivot_rules_deterministic(built):
     assert np.array_equal(a.objective.view(np.uint64), b.objective.view(np.uint64))
 
 
-@pytest.mark.skipif(not (REFERENCE / "benchmarks").exists(), reason="reference fixtures absent")
 def test_oracle_netlib(built, known_golden):
-    """The 8 Netlib LPs the reference ships (benchmarks/*.txt, read in place):
-    GLPK's verdict and its objective; listed Netlib optima to 1e-5."""
+    """The 8 Netlib LPs the reference ships (benchmarks/*.txt, committed copies
+    in tests/golden/netlib): GLPK's verdict and its objective; listed Netlib
+    optima to 1e-5."""
+    assert len(known_golden["netlib"]) == 8
     for name, v in known_golden["netlib"].items():
-        A, b, c = sp.read_abc(*(str(REFERENCE / "benchmarks" / f"{name}_{s}.txt") for s in "ABC"))
+        A, b, c = sp.read_abc(*(str(NETLIB / f"{name}_{s}.txt") for s in "ABC"))
         batch = sp.LPBatch.from_lps([(A, b, -c)])
         r = ref.solve_batch(batch, "fp64")
         assert r.status[0] == v["exact_status"], name
@@ -120,3 +121,11 @@ def test_family_sharing(built):
     full = sp.generate(3, 130, seed=9)
     for k in (0, 64, 129):
         assert np.array_equal(b.lp(k)[0], full.lp(k)[0])
+
+
+@pytest.mark.skipif(not (REFERENCE / "benchmarks").exists(), reason="reference checkout absent")
+def test_netlib_copies_match_reference():
+    """The committed Netlib files are byte-for-byte the reference's."""
+    for p in sorted(NETLIB.glob("*.txt")):
+        assert p.read_bytes() == (REFERENCE / "benchmarks" / p.name).read_bytes(), p.name
+    assert len(list(NETLIB.glob("*.txt"))) == 24

@@ -17,6 +17,7 @@ import pytest
 
 import simplexprojects_gb300 as sp
 from simplexprojects_gb300 import _native as N
+from oracle import ref as oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -40,11 +41,13 @@ def _device(batch):
     return d
 
 
-def _call(batch, d, precision):
+def _call(batch, d, precision, max_m=None, max_n=None):
     import torch
     p = lambda t: C.c_void_p(t.data_ptr())
+    max_m = int(batch.m.max()) if max_m is None else max_m
+    max_n = int(batch.n.max()) if max_n is None else max_n
     rc = N.lib().blpg_solve_noalloc(
-        batch.count, int(batch.m.max()), int(batch.n.max()), p(d["m"]), p(d["n"]), p(d["oA"]),
+        batch.count, max_m, max_n, p(d["m"]), p(d["n"]), p(d["oA"]),
         p(d["ob"]), p(d["oc"]), p(d["A"]), p(d["b"]), p(d["c"]), precision, p(d["status"]),
         p(d["obj"]), p(d["x"]), p(d["piv"]), C.c_void_p(torch.cuda.current_stream().cuda_stream))
     N.check(rc, "blpg_solve_noalloc")
@@ -53,29 +56,62 @@ def _call(batch, d, precision):
             d["x"].cpu().numpy())
 
 
+def _same(got, want, call=None):
+    st, obj, piv, x = got
+    assert np.array_equal(st, want.status), call
+    assert np.array_equal(piv, want.pivots), call
+    assert np.array_equal(obj.view(np.uint64), want.objective.view(np.uint64)), call
+    assert np.array_equal(x.view(np.uint64), want.x.view(np.uint64)), call
+
+
+@pytest.mark.parametrize("kind,count", [(1, 400), (4, 160)])
 @pytest.mark.parametrize("precision,name", [(0, "fp64"), (1, "fp32")])
-def test_noalloc_matches_solve_batch(built, precision, name):
-    batch = sp.generate(1, 400, seed=4242)
-    ref = sp.solve(batch, name, want_x=True)
+def test_noalloc_matches_solve_batch(built, kind, count, precision, name):
+    """Two calls in a row give blpg_solve_batch's bits.  Kind 4 mixes shapes
+    from m=16 to m=256: here every LP runs with the cluster size and thread
+    count of the largest, where blpg_solve_batch gives each its own size
+    class; the pivot rules do not depend on either."""
+    batch = sp.generate(kind, count, seed=4242 + kind)
+    want = sp.solve(batch, name, want_x=True)
     d = _device(batch)
     for call in range(2):
         d["status"].fill_(-9)
         d["obj"].fill_(float("nan"))
-        st, obj, piv, x = _call(batch, d, precision)
-        assert np.array_equal(st, ref.status), call
-        assert np.array_equal(piv, ref.pivots), call
-        assert np.array_equal(obj.view(np.uint64), ref.objective.view(np.uint64)), call
-        assert np.array_equal(x.view(np.uint64), ref.x.view(np.uint64)), call
+        _same(_call(batch, d, precision), want, call)
+    if precision == 0:  # and the FP64 oracle's, bit for bit
+        _same(_call(batch, d, precision), oracle.solve_batch(batch, "fp64", want_x=True))
 
 
-def test_noalloc_large_tableaux_use_clusters(built):
+@pytest.mark.parametrize("precision,name", [(0, "fp64"), (1, "fp32")])
+def test_noalloc_large_tableaux_use_clusters(built, precision, name):
     """Shapes that need a multi-CTA cluster give the same results too."""
     batch = sp.generate(2, 24, seed=99)
-    ref = sp.solve(batch, "fp64", want_x=True)
+    want = sp.solve(batch, name, want_x=True)
     d = _device(batch)
-    st, obj, piv, x = _call(batch, d, 0)
-    assert np.array_equal(st, ref.status) and np.array_equal(piv, ref.pivots)
-    assert np.array_equal(obj.view(np.uint64), ref.objective.view(np.uint64))
+    _same(_call(batch, d, precision), want)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_noalloc_refuses_phase_one_and_oversized_lps(built, precision):
+    """An LP with some b_i < 0 (phase I is not part of this entry point) and
+    an LP larger than the max_m / max_n passed get BLPG_UNDEF with pivots -1;
+    the other LPs of the call are solved as usual."""
+    base = sp.generate(0, 6, seed=7)
+    big = sp.generate(1, 1, seed=8)
+    lps = [base.lp(k) for k in range(6)]
+    A, b, c = base.lp(0)
+    b = b.copy()
+    b[3] = -1.0
+    lps.append((A, b, c))
+    lps.append(big.lp(0))
+    batch = sp.LPBatch.from_lps(lps)
+    d = _device(batch)
+    st, obj, piv, x = _call(batch, d, precision, max_m=28, max_n=32)
+    assert st[6] == 1 and piv[6] == -1
+    assert st[7] == 1 and piv[7] == -1
+    want = sp.solve(base, "fp32" if precision else "fp64")
+    assert np.array_equal(st[:6], want.status) and np.array_equal(piv[:6], want.pivots)
+    assert np.array_equal(obj[:6].view(np.uint64), want.objective.view(np.uint64))
 
 
 def test_noalloc_rejects_oversized_batches(built):
