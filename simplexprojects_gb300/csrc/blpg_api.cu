@@ -59,6 +59,7 @@ using dev::LpArgs;
 struct Tuning {
   std::mutex mu;
   std::map<std::pair<int, int>, int> threads;  // (precision*16 + K, size bucket)
+  int generation = 0;  // bumped by every blpg_set_tuning: cached plans are rebuilt
 };
 static Tuning g_tuning;
 
@@ -132,9 +133,6 @@ static void release(blpg_plan* p) {
 
 template <typename T, bool CL>
 static int set_kernel_attrs(int max_smem) {
-  static std::once_flag once[2];
-  static int rc = 0;
-  (void)once;
   cudaError_t e = cudaFuncSetAttribute(dev::solve_kernel<T, CL>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
   if (e != cudaSuccess)
@@ -145,7 +143,7 @@ static int set_kernel_attrs(int max_smem) {
     if (e != cudaSuccess)
       return fail(BLPG_ECUDA, "cluster attribute: %s", cudaGetErrorString(e));
   }
-  return rc;
+  return BLPG_OK;
 }
 
 template <typename T>
@@ -439,6 +437,7 @@ extern "C" const char* blpg_version(void) {
 extern "C" int32_t blpg_set_tuning(const char* json) {
   std::lock_guard<std::mutex> lk(g_tuning.mu);
   g_tuning.threads.clear();
+  ++g_tuning.generation;
   if (!json) return BLPG_OK;
   // Minimal reader for {"fp64_k1": 256, "fp32_k2": 512, "fp64_smem": 115712,
   // "fp32_ctas": 2, ...}: threads per CTA per (precision, cluster size), the
@@ -762,7 +761,13 @@ struct Workspace {
   std::vector<int32_t> key_negs;    // count of b_i < 0 per LP
   std::vector<int64_t> key_offs;
   blpg_options key_opt{};
+  int key_tuning = -1;  // tuning generation the cached plan was built with
 };
+
+static int tuning_generation() {
+  std::lock_guard<std::mutex> lk(g_tuning.mu);
+  return g_tuning.generation;
+}
 static Workspace g_ws;
 
 // The cached plan fits the batch's shapes, offsets and options (its
@@ -785,7 +790,7 @@ static bool plan_layout_matches(const Workspace& w, const blpg_batch* bt, const 
                                 const std::vector<int32_t>& shapes,
                                 const std::vector<int64_t>& offs) {
   return w.plan && same_plan_options(w.key_opt, o) && w.key_shapes == shapes &&
-         w.key_offs == offs && w.plan->count == bt->count;
+         w.key_offs == offs && w.plan->count == bt->count && w.key_tuning == tuning_generation();
 }
 }  // namespace blpg
 
@@ -913,6 +918,7 @@ extern "C" int32_t blpg_solve_batch(const blpg_batch* bt, const blpg_options* op
     g_ws.key_negs = negs;
     g_ws.key_offs = offs;
     g_ws.key_opt = opt;
+    g_ws.key_tuning = tuning_generation();
     if (!uploaded) {
       if ((rc = carve(g_ws.plan, sl)) || (rc = upload(g_ws.plan, sl))) return rc;
     }
