@@ -174,9 +174,16 @@ enum {
   BLPG_INFO_REFRESH = 16, /* FP64 refresh of the FP32 tableau ran */
   BLPG_INFO_REPAIR = 32,  /* an FP64 check found a violation: more pivots */
   BLPG_INFO_SHIFT = 64,   /* hinted basis infeasible both ways: cost-shifted dual phase */
-  BLPG_INFO_UNVERIFIED = 128 /* FP32: the FP64 refresh did not converge on the final
+  BLPG_INFO_UNVERIFIED = 128, /* FP32: the FP64 refresh did not converge on the final
                                 basis (the FP32 tableau is too inaccurate to check it);
                                 the status is BLPG_UNDEF */
+  BLPG_INFO_REINVERT = 256,  /* the tableau was rebuilt from an FP64 LU factorisation of
+                                its basis: before repair pivots when an FP64 check kept
+                                failing, or once in a long or degenerate FP32 solve
+                                (plans only) */
+  BLPG_INFO_FACTOR = 512     /* an FP64 refresh factorised the basis (LU) instead of
+                                refining through the tableau's B^-1: every phase-I LP,
+                                and bases the refinement could not settle (plans only) */
 };
 
 /* Fill *opt with the defaults above. */

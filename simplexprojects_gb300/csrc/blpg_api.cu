@@ -79,6 +79,8 @@ static int device_check(int device, cudaDeviceProp* prop) {
 
 struct ClassPlan {
   int K = 1, nt = 128, max_m = 0, max_na = 0, smem = 0;
+  int max_ns = 0;  // most structural basics any member can have: min(m, n)
+  long long lu_off = 0, lu_stride = 0;  // the class's LU refresh scratch (doubles)
   int ctas_per_sm = 1;
   int count = 0, grid = 0, order_off = 0;
   double work = 0;
@@ -101,6 +103,13 @@ struct blpg_plan {
   int32_t *d_m = nullptr, *d_n = nullptr, *d_order = nullptr, *d_tickets = nullptr;
   int64_t *d_off = nullptr;  // offA | offb | offc | offx | offbasis
   float* d_A32 = nullptr;    // FP32 plans: A rounded to FP32, elements [minA, extA) filled
+  double* d_lu = nullptr;    // LU refresh scratch of every class (FP32, FP64 steepest edge)
+  size_t lu_doubles = 0;
+  // FP32 plans: the FP64 pass, one persistent FP64 launch over the LPs the
+  // FP32 pass hands over (d_fb: [0] count, [1..] LP ids), usually none
+  bool has_fb = false;
+  blpg::ClassPlan fb_class;
+  int32_t* d_fb = nullptr;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_fork = nullptr;
   std::vector<cudaStream_t> aux;      // one per class after the first
@@ -123,6 +132,8 @@ static void release(blpg_plan* p) {
   cudaFree(p->d_tickets);
   cudaFree(p->d_off);
   cudaFree(p->d_A32);
+  cudaFree(p->d_lu);
+  cudaFree(p->d_fb);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
   if (p->ev_out) cudaEventDestroy(p->ev_out);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
@@ -297,6 +308,7 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
       c.smem = std::max(c.smem, items[lp].bytes);
       c.max_m = std::max(c.max_m, p->m[lp]);
       c.max_na = std::max(c.max_na, p->na[lp]);
+      c.max_ns = std::max(c.max_ns, std::min(p->m[lp], p->n[lp]));
       c.work += items[lp].work;
       nl = std::max(nl, items[lp].nl);
     }
@@ -340,6 +352,8 @@ static int launch_one(blpg_plan* p, size_t ci, const LpArgs& args, cudaStream_t 
   ca.max_na = c.max_na;
   ca.se = p->opt.pricing == BLPG_PRICE_STEEPEST ? 1 : 0;
   ca.smem = c.smem;
+  ca.lu = p->d_lu ? p->d_lu + c.lu_off : nullptr;
+  ca.lu_stride = c.lu_stride;
   if (c.K == 1) {
     dev::solve_kernel<T, false><<<c.grid, c.nt, c.smem, s>>>(args, ca);
     CK(cudaGetLastError());
@@ -357,6 +371,89 @@ static int launch_one(blpg_plan* p, size_t ci, const LpArgs& args, cudaStream_t 
     cfg.attrs = at;
     cfg.numAttrs = 1;
     CK(cudaLaunchKernelEx(&cfg, dev::solve_kernel<T, true>, args, ca));
+  }
+  return BLPG_OK;
+}
+
+// The FP64 pass of an FP32 plan: one class holding every LP of the plan in
+// the FP64 Dantzig layout (the reference's method, no LU verification), at
+// the smallest cluster size where the largest fits, launched after the FP32
+// classes over the device list they fill.  Returns false (no FP64 pass) when
+// some LP needs more than 8 CTAs in FP64.
+static bool build_fallback(blpg_plan* p, int max_smem) {
+  ClassPlan c;
+  for (int K = 1; K <= 8 && !c.smem; K *= 2) {
+    int smem = 0, nl = 1, max_na = 0;
+    bool fits = true;
+    for (int k = 0; k < p->count && fits; ++k) {
+      const int m = p->m[k], n = p->n[k], na = p->na[k];
+      Geom g(m, n, na, K, dev::VecT<double>::V);
+      const int bytes = Layout(m, g.ldw, n + m + na, 8, 0).total;
+      fits = bytes <= max_smem && g.nl <= kMaxThreads;
+      smem = std::max(smem, bytes);
+      nl = std::max(nl, g.nl);
+      max_na = std::max(max_na, na);
+    }
+    if (!fits) continue;
+    c.K = K;
+    c.smem = smem;
+    c.max_na = max_na;
+    c.nt = std::min(kMaxThreads, dev::round_up(std::max(nl, 256), 32));
+  }
+  if (!c.smem) return false;
+  int per_sm = 0, clusters = 0;
+  if (occupancy<double>(c, &per_sm, &clusters) != BLPG_OK) return false;
+  const int slots = c.K == 1 ? per_sm * p->sm_count : clusters;
+  if (slots <= 0) return false;
+  c.ctas_per_sm = c.K == 1 ? per_sm : 1;
+  c.grid = std::min({slots, std::max(1, p->count), 2 * p->sm_count}) * c.K;
+  p->fb_class = c;
+  return true;
+}
+
+static int launch_fallback(blpg_plan* p, const LpArgs& args, cudaStream_t s) {
+  const ClassPlan& c = p->fb_class;
+  LpArgs fa = args;
+  fa.opt_tol = 1e-9;
+  fa.piv_tol = 1e-7;
+  fa.feas_tol = 1e-9;
+  fa.phase1_tol = 1e-7;
+  fa.deg_tol = 1e-12;
+  fa.ptol = 1e-9;
+  fa.pricing = 0;
+  fa.weight = nullptr;
+  fa.A32 = nullptr;
+  fa.hint = nullptr;
+  fa.refresh_period = 0;
+  fa.fb = nullptr;
+  fa.info_or = dev::kInfoFp64;
+  ClassArgs ca{};
+  ca.order = p->d_fb + 1;
+  ca.count = 0;
+  ca.count_dev = p->d_fb;
+  ca.ticket = p->d_tickets + p->classes.size();
+  ca.K = c.K;
+  ca.max_na = c.max_na;
+  ca.se = 0;
+  ca.smem = c.smem;
+  ca.lu = nullptr;
+  if (c.K == 1) {
+    dev::solve_kernel<double, false><<<c.grid, c.nt, c.smem, s>>>(fa, ca);
+    CK(cudaGetLastError());
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = c.K;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(c.grid, 1, 1);
+    cfg.blockDim = dim3(c.nt, 1, 1);
+    cfg.dynamicSmemBytes = c.smem;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    CK(cudaLaunchKernelEx(&cfg, dev::solve_kernel<double, true>, fa, ca));
   }
   return BLPG_OK;
 }
@@ -384,7 +481,8 @@ __global__ void round_f32_kernel(const double* __restrict__ in, float* __restric
 
 template <typename T>
 static int launch_classes(blpg_plan* p, const LpArgs& args, cudaStream_t s) {
-  CK(cudaMemsetAsync(p->d_tickets, 0, sizeof(int32_t) * std::max<size_t>(1, p->classes.size()), s));
+  CK(cudaMemsetAsync(p->d_tickets, 0, sizeof(int32_t) * (p->classes.size() + 1), s));
+  if (args.fb) CK(cudaMemsetAsync(args.fb, 0, sizeof(int32_t), s));
   const size_t nc = p->classes.size();
   if (nc == 0) return BLPG_OK;
   if (args.A32) {  // A rounded to FP32 before any class loads a tableau
@@ -404,6 +502,7 @@ static int launch_classes(blpg_plan* p, const LpArgs& args, cudaStream_t s) {
     CK(cudaEventRecord(p->ev_join[ci - 1], p->aux[ci - 1]));
     CK(cudaStreamWaitEvent(s, p->ev_join[ci - 1], 0));
   }
+  if (args.fb) return launch_fallback(p, args, s);  // after every FP32 class
   return BLPG_OK;
 }
 
@@ -532,6 +631,8 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
   if (p->precision == BLPG_FP32) {
     if ((rc = set_kernel_attrs<float, false>(max_smem))) return rc;
     if ((rc = set_kernel_attrs<float, true>(max_smem))) return rc;
+    if ((rc = set_kernel_attrs<double, false>(max_smem))) return rc;  // the FP64 pass
+    if ((rc = set_kernel_attrs<double, true>(max_smem))) return rc;
     rc = build_classes<float>(p.get(), max_smem, opt.max_cluster);
   } else {
     if ((rc = set_kernel_attrs<double, false>(max_smem))) return rc;
@@ -570,7 +671,7 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
   CKF(cudaMalloc(&p->d_m, sizeof(int32_t) * Nn));
   CKF(cudaMalloc(&p->d_n, sizeof(int32_t) * Nn));
   CKF(cudaMalloc(&p->d_order, sizeof(int32_t) * Nn));
-  CKF(cudaMalloc(&p->d_tickets, sizeof(int32_t) * nc));
+  CKF(cudaMalloc(&p->d_tickets, sizeof(int32_t) * (nc + 1)));  // + the FP64 pass's
   CKF(cudaMalloc(&p->d_off, sizeof(int64_t) * 6 * Nn));
   // FP32 tableaux load A from an FP32 copy rounded once per execute (one
   // bandwidth-bound pass) when LPs share A: every element of A's extent read
@@ -582,6 +683,30 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
   if (p->precision == BLPG_FP32 && p->extA > p->minA && readA >= 2 * (p->extA - p->minA)) {
     CKF(cudaMalloc(&p->d_A32, sizeof(float) * (size_t)p->extA));
     p->launches += 1;
+  }
+  if (p->precision == BLPG_FP32 && N > 0 && build_fallback(p.get(), max_smem)) {
+    CKF(cudaMalloc(&p->d_fb, sizeof(int32_t) * (size_t)(N + 1)));
+    p->has_fb = true;
+    p->launches += 1;
+  }
+  // FP64 scratch of the LU refresh (FP32 plans, FP64 plans with steepest
+  // edge): per persistent CTA (cluster) of a class, the kernel matrix of the
+  // largest possible basis (min(m, n) structural basics), five vectors and
+  // two per warp (the rebuild solves a column per warp), rounded to 32
+  // doubles; plans whose scratch would pass 4 GiB refresh by iterative
+  // refinement only
+  if (p->precision == BLPG_FP32 || p->opt.pricing == BLPG_PRICE_STEEPEST) {
+    size_t total = 0;
+    for (auto& c : p->classes) {
+      const long long ns = std::max(1, c.max_ns);
+      c.lu_stride = (ns * ns + (5 + 2 * (kMaxThreads / 32)) * ns + 31) / 32 * 32;
+      c.lu_off = (long long)total;
+      total += (size_t)c.lu_stride * (size_t)(c.grid / std::max(1, c.K));
+    }
+    if (total > 0 && total * sizeof(double) <= (size_t(4) << 30)) {
+      CKF(cudaMalloc(&p->d_lu, sizeof(double) * total));
+      p->lu_doubles = total;
+    }
   }
   if (N > 0) {
     std::vector<int64_t> off(6 * (size_t)N);
@@ -639,6 +764,7 @@ extern "C" int32_t blpg_plan_execute_weighted(blpg_plan* p, const double* dA, co
   a.weight = price_weight;
   a.A = dA;
   a.A32 = p->d_A32;
+  a.fb = p->has_fb ? p->d_fb : nullptr;
   a.b = db;
   a.c = dc;
   a.status = out->status;

@@ -83,6 +83,8 @@ struct LpArgs {
   const float* weight;     // nullable: steepest-edge score weight per variable (n + m per LP)
   const int64_t* offw;     // offsets of `weight`
   const float* A32;        // nullable: A rounded to FP32 (offsets of A), read by FP32 tableau loads
+  int32_t* fb;             // nullable (FP32 plans): [0] count, [1..] LPs handed to the FP64 pass
+  int32_t info_or;         // bits OR'ed into every info written (the FP64 pass: kInfoFp64)
 };
 
 // Bits of the per-LP info output.
@@ -94,15 +96,21 @@ constexpr int kInfoRefresh = 16;   // FP64 refresh of the FP32 tableau ran
 constexpr int kInfoRepair = 32;    // a refresh found a violation (more pivots)
 constexpr int kInfoShift = 64;     // hinted basis infeasible both ways: cost-shifted dual phase
 constexpr int kInfoUnverified = 128;  // FP32: the FP64 refresh could not verify the final basis
+constexpr int kInfoReinvert = 256;    // the tableau was rebuilt from an FP64 factorisation
+constexpr int kInfoFactor = 512;      // an FP64 refresh used the LU factorisation (refresh_lu)
+constexpr int kInfoFp64 = 1024;       // re-solved on an FP64 tableau (the FP64 pass of an FP32 plan)
 
 struct ClassArgs {
   const int32_t* order;  // LP ids of this class, heaviest first
   int32_t count;
+  const int32_t* count_dev;  // nullable: the count in device memory (the FP64 pass's list)
   int32_t* ticket;  // queue head, zeroed before the launch
   int32_t K;        // CTAs per LP (cluster size)
   int32_t max_na;   // artificial columns (two-phase LPs); LPs with more are refused
   int32_t se;       // steepest-edge pricing: the layout holds column norms
   int32_t smem;     // dynamic shared memory per CTA; LPs whose layout is larger are refused
+  double* lu;          // nullable: FP64 scratch of the LU refresh, lu_stride doubles per
+  long long lu_stride; // CTA (per cluster: the cluster's index blockIdx.x / K)
 };
 
 template <typename T>
@@ -170,8 +178,9 @@ struct Layout {
     vpos = off;  // slot of every nonbasic variable, -1 - row of a basic one
     off += nvp * 4;
     ext = off;
-    // FP32 tableau: FP64 x_B and duals of the refresh, FP32 residual copy
-    const int ext_bytes = elem == 4 ? 2 * mp1 * 8 + mp1 * 4 : 0;
+    // FP64 x_B, duals and a 32-bit list of the refresh (FP32 tableaux, and
+    // FP64 ones with steepest edge, which are verified in FP64 too)
+    const int ext_bytes = (elem == 4 || se) ? 2 * mp1 * 8 + mp1 * 4 : 0;
     off += ext_bytes;
     // steepest edge: two 32-bit fixed-point norm counters per local column slot,
     // sharing the refresh's region when it is large enough (the norms are
@@ -446,9 +455,10 @@ struct Solver {
   int* cvar;   // slot -> variable id (every slot of the LP, replicated per CTA)
   int* vpos;   // variable -> slot if nonbasic, -1 - row if basic
   uint2* gam;  // steepest edge: fixed-point column norms of the local slots
-  double* xr;  // FP32 tableau only: FP64 x_B of the refresh
-  double* yr;  // FP32 tableau only: FP64 duals of the refresh
-  float* rf;   // FP32 tableau only: the refresh's residuals rounded to FP32
+  double* xr;  // FP64 x_B of the refresh (FP32 tableaux, FP64 ones with steepest edge)
+  double* yr;  // FP64 duals of the refresh
+  float* rf;   // the refresh's residuals rounded to FP32 / a 32-bit list
+  double* lu;  // nullable: this CTA's FP64 scratch for the LU refresh (global memory)
   Key* redP;
   Key* redR;
   Key* redH;
@@ -1222,6 +1232,443 @@ struct Solver {
     return i == -1 - v ? T(1) : T(0);
   }
 
+  // FP64 refresh by refactorisation of the basis.  With the basis's
+  // structural columns J (ns of them, in tableau-row order) and the
+  // constraints R not covered by a basic slack or a basic artificial (ns of
+  // them, in increasing order), the basis matrix in the original coordinates
+  // is, up to a permutation, [[K, 0], [A[C, J], D]] with K = A[R, J] and D
+  // diagonal (+1 for a basic slack, -1 for a basic artificial: the
+  // artificial of a row with b_i < 0 carries +1 in the negated row).  So
+  //   K x_J = b_R,  x of the basic slack (artificial) of constraint k =
+  //   +(-)(b_k - A[k, J] x_J);   K^T y_R = c_J,  y = 0 off R;
+  //   d_j = y_R^T A[R, j] - c_j (structural),  d = y_k (slack k),
+  //   z = c_J^T x_J.
+  // K is factorised in FP64 with partial pivoting (one warp, K in the CTA's
+  // global scratch, rows permuted through a list), each solve is refined once
+  // from an FP64 residual on the original A, and the correction judges the
+  // factorisation: it must be <= 1e-9 of the values, else bit 2 is clear (the
+  // basis is singular or too ill-conditioned to verify).  Nothing is read
+  // from the tableau except the basis, so the accuracy of x, y and d does not
+  // depend on the FP32 values, and rows negated for phase I need no special
+  // case.  The RHS column (every replica) and the objective row are
+  // overwritten as in refresh_refine; the artificials' reduced costs are not
+  // (they are never priced after phase I).  Rank 0 computes; every sum runs
+  // in a fixed order, independent of the thread count and the cluster split.
+  // Returns the bits of refresh_refine.  Out of line with the geometry by
+  // value: it runs once or twice per LP.
+  __device__ __noinline__ int refresh_lu(const Geom g, const double* A, const double* b,
+                                         const double* c, const double opt_tol,
+                                         const double ptol) {
+    const int m = g.m, n = g.n, na = g.na;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    const unsigned full = 0xffffffffu;
+    if (CLUSTER) csync();
+    int ok = 0;
+    if (rank == 0) {
+      int* slist = flags;                          // rows of the structural basics
+      int* rlist = reinterpret_cast<int*>(rhsx);   // uncovered constraints R
+      int* perm = reinterpret_cast<int*>(rf);      // LU row order (positions in R)
+      int* arow = reinterpret_cast<int*>(col0);    // constraint of each artificial
+      int* wcount = reinterpret_cast<int*>(redH);  // chunk offsets: [0,33) rows, [64,97) R
+      const int nch = ceil_div(m, 32);
+      // artificial a belongs to the a-th constraint with b_i < 0 (load())
+      if (na > 0) {
+        for (int ch = warp; ch < nch; ch += nw) {
+          const int i = ch * 32 + lane;
+          const unsigned bal = __ballot_sync(full, i < m && b[i] < 0.0);
+          if (lane == 0) wcount[ch] = __popc(bal);
+        }
+        __syncthreads();
+        if (tid == 0) {
+          int acc = 0;
+          for (int ch = 0; ch < nch; ++ch) {
+            const int v = wcount[ch];
+            wcount[ch] = acc;
+            acc += v;
+          }
+        }
+        __syncthreads();
+        for (int ch = warp; ch < nch; ch += nw) {
+          const int i = ch * 32 + lane;
+          const bool neg = i < m && b[i] < 0.0;
+          const unsigned bal = __ballot_sync(full, neg);
+          if (neg) arow[wcount[ch] + __popc(bal & ((1u << lane) - 1u))] = i;
+        }
+        __syncthreads();
+      }
+      // yr[k] = 1 marks constraint k covered: its slack, or its artificial, is basic
+      for (int k = tid; k < m; k += nt) yr[k] = vpos[n + k] < 0 ? 1.0 : 0.0;
+      __syncthreads();
+      for (int i = tid; i < m; i += nt) {
+        const int v = basis[i];
+        if (v >= n + m) yr[arow[v - n - m]] = 1.0;
+      }
+      __syncthreads();
+      // the lists, by ballots and prefix sums over 32-row chunks
+      for (int ch = warp; ch < 2 * nch; ch += nw) {
+        const bool rows = ch < nch;
+        const int i = (rows ? ch : ch - nch) * 32 + lane;
+        const bool st = i < m && (rows ? basis[i] < n : yr[i] == 0.0);
+        const unsigned bal = __ballot_sync(full, st);
+        if (lane == 0) wcount[rows ? ch : 64 + ch - nch] = __popc(bal);
+      }
+      __syncthreads();
+      if (tid < 2) {
+        int acc = 0;
+        for (int ch = 0; ch < nch; ++ch) {
+          const int v = wcount[64 * tid + ch];
+          wcount[64 * tid + ch] = acc;
+          acc += v;
+        }
+        wcount[64 * tid + nch] = acc;
+      }
+      __syncthreads();
+      for (int ch = warp; ch < 2 * nch; ch += nw) {
+        const bool rows = ch < nch;
+        const int i = (rows ? ch : ch - nch) * 32 + lane;
+        const bool st = i < m && (rows ? basis[i] < n : yr[i] == 0.0);
+        const unsigned bal = __ballot_sync(full, st);
+        const int pos = __popc(bal & ((1u << lane) - 1u));
+        if (st) {
+          if (rows)
+            slist[wcount[ch] + pos] = i;
+          else
+            rlist[wcount[64 + ch - nch] + pos] = i;
+        }
+      }
+      __syncthreads();
+      const int ns = wcount[nch], nr = wcount[64 + nch];
+      // global scratch: K (ns x ns, row-major, rows in R order), then vectors
+      double* Km = lu;
+      double* xJ = Km + (size_t)ns * ns;  // x_J (J order)
+      double* yR = xJ + ns;               // y_R (R order)
+      double* v1 = yR + ns;               // right-hand sides, then corrections
+      double* v2 = v1 + ns;
+      double* v3 = v2 + ns;               // solve scratch
+      bool good = ns == nr;
+      if (good) {
+        for (int e = tid; e < ns * ns; e += nt) {
+          const int r = e / ns, cc = e - r * ns;
+          Km[e] = __ldg(A + (size_t)rlist[r] * n + basis[slist[cc]]);
+        }
+        for (int t = tid; t < ns; t += nt) {
+          v1[t] = __ldg(b + rlist[t]);
+          v2[t] = __ldg(c + basis[slist[t]]);
+        }
+      }
+      __syncthreads();
+      // ---- LU with partial pivoting and the solves, by warp 0
+      if (warp == 0) {
+        bool conv = false;
+        if (good) {
+          for (int r = lane; r < ns; r += 32) perm[r] = r;
+          __syncwarp();
+          double kmax = 0.0;  // largest |K| entry, for the singularity threshold
+          for (int e = lane; e < ns * ns; e += 32) kmax = fmax(kmax, fabs(Km[e]));
+          for (int o = 16; o > 0; o >>= 1) kmax = fmax(kmax, __shfl_xor_sync(full, kmax, o));
+          const double tiny = 1e-13 * kmax;
+          for (int kk = 0; kk < ns; ++kk) {
+            double bv = -1.0;
+            int bi = ns;
+            for (int i = kk + lane; i < ns; i += 32) {
+              const double v = fabs(Km[(size_t)perm[i] * ns + kk]);
+              if (v > bv) {
+                bv = v;
+                bi = i;
+              }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+              const double ov = __shfl_xor_sync(full, bv, o);
+              const int oi = __shfl_xor_sync(full, bi, o);
+              if (ov > bv || (ov == bv && oi < bi)) {
+                bv = ov;
+                bi = oi;
+              }
+            }
+            if (!(bv > tiny)) {  // singular (warp-uniform)
+              good = false;
+              break;
+            }
+            const int pb = perm[bi];
+            __syncwarp();
+            if (lane == 0) {
+              perm[bi] = perm[kk];
+              perm[kk] = pb;
+            }
+            __syncwarp();
+            const double* urow = Km + (size_t)pb * ns;
+            const double rinv = 1.0 / urow[kk];
+            for (int i = kk + 1 + lane; i < ns; i += 32)
+              Km[(size_t)perm[i] * ns + kk] *= rinv;  // the multiplier, in L's place
+            __syncwarp();
+            const int w = ns - kk - 1;
+            for (int e = lane; e < w * w; e += 32) {
+              const int i = kk + 1 + e / w, cc = kk + 1 + e % w;
+              double* row = Km + (size_t)perm[i] * ns;
+              row[cc] = fma(-row[kk], urow[cc], row[cc]);
+            }
+            __syncwarp();
+          }
+        }
+        if (good) {
+          // K x = v1 (x_J) and K^T y = v2 (y_R), refined from residuals on
+          // the original A until the correction is below 1e-12 of the values
+          // (at most three refinement steps); converged when the last one is
+          // below 1e-9
+          double cx = 0.0, mx = 0.0, cy = 0.0, my = 0.0;
+          for (int pass = 0; pass < 4; ++pass) {
+            lu_solve(Km, perm, ns, v1, v3, lane);    // v1 <- K^-1 v1
+            lu_solve_t(Km, perm, ns, v2, v3, lane);  // v2 <- K^-T v2
+            for (int t = lane; t < ns; t += 32) {
+              if (pass == 0) {
+                xJ[t] = v1[t];
+                yR[t] = v2[t];
+              } else {
+                xJ[t] += v1[t];
+                yR[t] += v2[t];
+              }
+            }
+            __syncwarp();
+            if (pass > 0) {
+              cx = cy = mx = my = 0.0;
+              for (int t = lane; t < ns; t += 32) {
+                cx = fmax(cx, fabs(v1[t]));
+                cy = fmax(cy, fabs(v2[t]));
+                mx = fmax(mx, fabs(xJ[t]));
+                my = fmax(my, fabs(yR[t]));
+              }
+              for (int o = 16; o > 0; o >>= 1) {
+                cx = fmax(cx, __shfl_xor_sync(full, cx, o));
+                cy = fmax(cy, __shfl_xor_sync(full, cy, o));
+                mx = fmax(mx, __shfl_xor_sync(full, mx, o));
+                my = fmax(my, __shfl_xor_sync(full, my, o));
+              }
+              if (pass == 3 || (cx <= 1e-12 * fmax(1.0, mx) && cy <= 1e-12 * fmax(1.0, my)))
+                break;
+            }
+            // residuals b_R - K x_J and c_J - K^T y_R from the original A
+            for (int t = lane; t < ns; t += 32) {
+              const double* Ar = A + (size_t)rlist[t] * n;
+              const int jt = basis[slist[t]];
+              double s0 = 0.0, s1 = 0.0;
+              for (int u = 0; u < ns; ++u) {
+                s0 = fma(__ldg(Ar + basis[slist[u]]), xJ[u], s0);
+                s1 = fma(__ldg(A + (size_t)rlist[u] * n + jt), yR[u], s1);
+              }
+              v1[t] = __ldg(b + rlist[t]) - s0;
+              v2[t] = __ldg(c + jt) - s1;
+            }
+            __syncwarp();
+          }
+          conv = cx <= 1e-9 * fmax(1.0, mx) && cy <= 1e-9 * fmax(1.0, my);
+        }
+        if (lane == 0) sh->aux.w1 = (good ? 1u : 0u) | (conv ? 2u : 0u);
+      }
+      __syncthreads();
+      good = (sh->aux.w1 & 1u) != 0u;
+      const bool conv = (sh->aux.w1 & 2u) != 0u;
+      bool badd = false, badp = false;
+      if (good) {
+        // y per constraint (0 off R) and x per tableau row
+        for (int k = tid; k < m; k += nt) yr[k] = 0.0;
+        __syncthreads();
+        for (int t = tid; t < ns; t += nt) {
+          yr[rlist[t]] = yR[t];
+          xr[slist[t]] = xJ[t];
+        }
+        for (int i = tid; i < m; i += nt) {
+          const int v = basis[i];
+          if (v < n) continue;
+          const bool art = v >= n + m;
+          const int k = art ? arow[v - n - m] : v - n;
+          const double* Ak = A + (size_t)k * n;
+          double s0 = 0.0;
+          for (int u = 0; u < ns; ++u) s0 = fma(__ldg(Ak + basis[slist[u]]), xJ[u], s0);
+          const double xv = __ldg(b + k) - s0;
+          xr[i] = art ? -xv : xv;
+        }
+        __syncthreads();
+        // reduced costs of the nonbasic structurals and slacks
+        for (int j = tid; j < n; j += nt) {
+          const int sv = vpos[j];
+          if (sv < 0) continue;
+          double s0 = 0.0;
+          for (int t = 0; t < ns; ++t) s0 = fma(__ldg(A + (size_t)rlist[t] * n + j), yR[t], s0);
+          const double d = s0 - __ldg(c + j);
+          *elem(g, m, sv) = (T)d;
+          badd = badd || d < -opt_tol;
+        }
+        for (int k = tid; k < m; k += nt) {
+          const int sv = vpos[n + k];
+          if (sv < 0) continue;
+          const double d = yr[k];
+          *elem(g, m, sv) = (T)d;
+          badd = badd || d < -opt_tol;
+        }
+        for (int i = tid; i < m; i += nt) {
+          const T xv = (T)xr[i];
+          for (int o = 0; o < K; ++o) {
+            T* p = tab + (size_t)i * g.ldw + g.cw;
+            *(o == rank ? p : remote(p, o)) = xv;
+          }
+          badp = badp || xr[i] < -ptol;
+        }
+        if (warp == 0) {  // z = c_J^T x_J, lane-strided partial sums and a butterfly
+          double z = 0.0;
+          for (int t = lane; t < ns; t += 32) z = fma(__ldg(c + basis[slist[t]]), xJ[t], z);
+          for (int o = 16; o > 0; o >>= 1) z += __shfl_xor_sync(full, z, o);
+          if (lane == 0) {
+            sh->z = z;
+            for (int o = 0; o < K; ++o) {
+              T* p = tab + (size_t)m * g.ldw + g.cw;
+              *(o == rank ? p : remote(p, o)) = (T)z;
+            }
+          }
+        }
+      }
+      badd = __syncthreads_or(badd ? 1 : 0) != 0;
+      badp = __syncthreads_or(badp ? 1 : 0) != 0;
+      ok = good ? ((badp ? 0 : 1) | (badd ? 0 : 2) | (conv ? 4 : 0)) : 0;
+      if (tid == 0) sh->aux.w1 = (unsigned)ok;
+    }
+    if (CLUSTER) {
+      csync();
+      ok = (int)remote(&sh->aux, 0)->w1;
+      csync();
+    }
+    return ok;
+  }
+
+  // x <- K^-1 x with PK = LU stored in K (the multipliers of L below the
+  // diagonal, unit diagonal implied; row i of PK is row perm[i] of K); one
+  // warp, column-oriented substitutions, w (ns doubles) scratch.
+  static __device__ void lu_solve(const double* K, const int* perm, int ns, double* x, double* w,
+                                  int lane) {
+    for (int i = lane; i < ns; i += 32) w[i] = x[perm[i]];
+    __syncwarp();
+    for (int k = 0; k < ns; ++k) {  // L z = P x
+      const double wk = w[k];
+      for (int i = k + 1 + lane; i < ns; i += 32)
+        w[i] = fma(-K[(size_t)perm[i] * ns + k], wk, w[i]);
+      __syncwarp();
+    }
+    for (int k = ns - 1; k >= 0; --k) {  // U x = z
+      const double wk = w[k] / K[(size_t)perm[k] * ns + k];
+      __syncwarp();
+      if (lane == 0) w[k] = wk;
+      for (int i = lane; i < k; i += 32) w[i] = fma(-K[(size_t)perm[i] * ns + k], wk, w[i]);
+      __syncwarp();
+    }
+    for (int i = lane; i < ns; i += 32) x[i] = w[i];
+    __syncwarp();
+  }
+
+  // x <- K^-T x: K^T = U^T L^T P, so U^T s = x (forward), L^T u = s
+  // (backward) and x[perm[i]] = u[i]; one warp, w (ns doubles) scratch.
+  static __device__ void lu_solve_t(const double* K, const int* perm, int ns, double* x,
+                                    double* w, int lane) {
+    for (int i = lane; i < ns; i += 32) w[i] = x[i];
+    __syncwarp();
+    for (int k = 0; k < ns; ++k) {
+      const double* urow = K + (size_t)perm[k] * ns;
+      const double wk = w[k] / urow[k];
+      __syncwarp();
+      if (lane == 0) w[k] = wk;
+      for (int j = k + 1 + lane; j < ns; j += 32) w[j] = fma(-urow[j], wk, w[j]);
+      __syncwarp();
+    }
+    for (int k = ns - 1; k >= 0; --k) {
+      const double* lrow = K + (size_t)perm[k] * ns;
+      const double wk = w[k];
+      for (int i = lane; i < k; i += 32) w[i] = fma(-lrow[i], wk, w[i]);
+      __syncwarp();
+    }
+    for (int i = lane; i < ns; i += 32) x[perm[i]] = w[i];
+    __syncwarp();
+  }
+
+  // The FP64 refresh: iterative refinement through the tableau's B^-1 (the
+  // fast path, FP64 work proportional to the structural basics), or, with LU
+  // scratch (plans; the allocation-free entry point has none), the
+  // factorisation of refresh_lu for every phase-I LP and whenever the
+  // refinement does not converge.  Bit 3 of the result: the LU factors of
+  // the current basis are in the scratch (reinvert may use them).
+  __device__ int refresh(const Geom& g, const double* A, const double* b, const double* c,
+                         const LpArgs& a) {
+    if (g.na == 0 || !lu) {
+      const int ok = refresh_refine(g, A, b, c, a.opt_tol, a.ptol);
+      if ((ok & 4) || !lu) return ok;
+    }
+    const int ok = refresh_lu(g, A, b, c, a.opt_tol, a.ptol);
+    return ok | ((ok & 4) ? 8 : 0);
+  }
+
+  // Rebuild the tableau of the current basis from its FP64 factorisation
+  // (left in the scratch and the lists by refresh_lu): every slot's column
+  // is B^-1 a_j in the original coordinates (the negated phase-I rows cancel
+  // out: (D B)^-1 D a_j = B^-1 a_j), i.e. u_J = K^-1 a_j[R] on the rows of
+  // the structural basics and +-(a_jk - A[k, J] u_J) on the row holding the
+  // slack (+) or artificial (-) of constraint k.  One warp per column, FP64
+  // solves, entries rounded to the tableau's type; the RHS and the objective
+  // row were set by refresh_lu.  Used before repair pivots, when the tableau
+  // has drifted too far from its basis for the repairs to be trusted.
+  __device__ __noinline__ void reinvert(const Geom g, const double* A) {
+    const int m = g.m, n = g.n;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    if (CLUSTER) csync();
+    if (rank == 0) {
+      const int* slist = flags;
+      const int* rlist = reinterpret_cast<const int*>(rhsx);
+      const int* perm = reinterpret_cast<const int*>(rf);
+      const int* arow = reinterpret_cast<const int*>(col0);
+      int* rowpos = reinterpret_cast<int*>(yr);  // tableau row -> position in J (or -1)
+      int ns = 0;
+      for (int i = tid; i < m; i += nt) ns += basis[i] < n ? 1 : 0;
+      ns = block_sum(ns);
+      for (int i = tid; i < m; i += nt) rowpos[i] = -1;
+      __syncthreads();
+      for (int t = tid; t < ns; t += nt) rowpos[slist[t]] = t;
+      __syncthreads();
+      const double* Km = lu;
+      double* v = lu + (size_t)ns * ns + 5 * (size_t)ns + (size_t)warp * 2 * ns;
+      double* w = v + ns;
+      for (int sl = warp; sl < g.Wc; sl += nw) {
+        const int j = cvar[sl];
+        // a_j on the uncovered constraints R
+        for (int t = lane; t < ns; t += 32) {
+          const int k = rlist[t];
+          v[t] = j < n ? __ldg(A + (size_t)k * n + j)
+                       : (j < n + m ? (j - n == k ? 1.0 : 0.0) : (arow[j - n - m] == k ? -1.0 : 0.0));
+        }
+        __syncwarp();
+        lu_solve(Km, perm, ns, v, w, lane);
+        for (int i = lane; i < m; i += 32) {
+          const int bi = basis[i];
+          double u;
+          if (bi < n) {
+            u = v[rowpos[i]];
+          } else {
+            const bool art = bi >= n + m;
+            const int k = art ? arow[bi - n - m] : bi - n;
+            const double ajk =
+                j < n ? __ldg(A + (size_t)k * n + j)
+                      : (j < n + m ? (j - n == k ? 1.0 : 0.0) : (arow[j - n - m] == k ? -1.0 : 0.0));
+            double s0 = 0.0;
+            for (int t = 0; t < ns; ++t)
+              s0 = fma(__ldg(A + (size_t)k * n + basis[slist[t]]), v[t], s0);
+            u = art ? -(ajk - s0) : ajk - s0;
+          }
+          *elem(g, i, sl) = (T)u;
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    if (CLUSTER) csync();
+  }
+
   // FP64 refresh of the FP32 tableau: x_B and the duals y are recomputed
   // from the original A, b, c with iterative refinement (residual in FP64,
   // correction through B^-1 in FP32; the columns of B^-1 are the slack
@@ -1236,8 +1683,9 @@ struct Solver {
   // dot product per nonbasic structural column.  Returns bit 0: x_B >= -ptol,
   // bit 1: d >= -opt_tol (both judged in FP64), bit 2: both refinements
   // converged (without it bits 0 and 1 prove nothing).  Single-phase LPs only.
-  __device__ int refresh(const Geom& g, const double* A, const double* b, const double* c,
-                         const LpArgs& a) {
+  __device__ __noinline__ int refresh_refine(const Geom g, const double* A, const double* b,
+                                             const double* c, const double opt_tol,
+                                             const double ptol) {
     const int m = g.m, n = g.n;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
@@ -1465,14 +1913,14 @@ struct Solver {
         for (; k < m; ++k) p0 = fma(__ldg(A + (size_t)k * n + j), yr[k], p0);
         const double d = ((p0 + p1) + (p2 + p3)) - c[j];
         *elem(g, m, sv) = (T)d;
-        badd = badd || d < -a.opt_tol;
+        badd = badd || d < -opt_tol;
       }
       for (int k = tid; k < m; k += nt) {
         const int sv = vpos[n + k];
         if (sv < 0) continue;
         const double d = yr[k];
         *elem(g, m, sv) = (T)d;
-        badd = badd || d < -a.opt_tol;
+        badd = badd || d < -opt_tol;
       }
       for (int i = tid; i < m; i += nt) {
         const T xv = (T)xr[i];
@@ -1480,7 +1928,7 @@ struct Solver {
           T* p = tab + (size_t)i * g.ldw + g.cw;
           *(o == rank ? p : remote(p, o)) = xv;
         }
-        badp = badp || xr[i] < -a.ptol;
+        badp = badp || xr[i] < -ptol;
       }
       // z = c_B^T x_B: warp 0, lane-strided partial sums over the structural
       // basics combined by a butterfly (a fixed order)
@@ -1717,6 +2165,57 @@ struct Solver {
     __syncthreads();
   }
 
+  // Verify an optimal basis in FP64 and repair it if needed: a refresh,
+  // then, while it finds a violation, dual simplex (x_B < 0) and primal
+  // simplex pivots, each round verified by another refresh (at most four
+  // repairs).  Returns kOpt once verified, kUnverified when a refresh cannot
+  // judge the basis (or four repairs do not settle it), or the status a
+  // repair ended on.
+  __device__ int verify_basis(const Geom& g, int c0, int lc, const double* A, const double* b,
+                              const double* c, const LpArgs& a, const float* w, int budget,
+                              int& pivots, bool& bland, int& degen, int& cur, int& piv_fresh,
+                              int& info) {
+    const T ptol = (T)a.ptol;
+    int st = kOpt;
+    bool verified = false;
+    for (int round = 0; round <= 4; ++round) {
+      if (CLUSTER) csync();
+      int fl = refresh(g, A, b, c, a);
+      piv_fresh = pivots;
+      info |= kInfoRefresh | ((fl & 8) ? kInfoFactor : 0);
+      if ((fl & 7) == 7) {
+        verified = true;
+        break;
+      }
+      if (!(fl & 4)) break;  // no refresh could judge the basis
+      if (round == 4) break;
+      info |= kInfoRepair;
+      if (lu && (round > 0 || (fl & 8))) {
+        // the first repair on the tableau as it is did not settle the basis,
+        // or its B^-1 could not even be refined: repairs on a tableau rebuilt
+        // from the basis's FP64 factorisation
+        if (!(fl & 8)) fl = refresh_lu(g, A, b, c, a.opt_tol, a.ptol) | 8;
+        info |= kInfoFactor;
+        if (!(fl & 4)) break;
+        if ((fl & 3) == 3) {
+          verified = true;
+          break;
+        }
+        reinvert(g, A);
+        info |= kInfoReinvert;
+      }
+      if (!(fl & 1)) {
+        info |= kInfoDual;
+        st = dual_loop(g, c0, lc, a, budget, pivots, cur, ptol);
+        if (st != kOpt) break;
+      }
+      st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
+      if (st != kOpt) break;
+    }
+    if (st == kOpt && !verified) st = kUnverified;
+    return st;
+  }
+
   // Per-LP regions of the shared-memory layout.
   __device__ void place(const Layout& L, int m) {
     tab = reinterpret_cast<T*>(smem + L.tab);
@@ -1736,6 +2235,7 @@ struct Solver {
   __device__ void run(const LpArgs& a, const ClassArgs& ca) {
     const int tid = threadIdx.x, nt = blockDim.x;
     constexpr bool kFP32 = sizeof(T) == 4;
+    const int count = ca.count_dev ? *ca.count_dev : ca.count;
     for (;;) {
       if (rank == 0 && tid == 0) sh->ticket = atomicAdd(ca.ticket, 1);
       csync();
@@ -1745,7 +2245,7 @@ struct Solver {
         __syncthreads();
       }
       const int t = sh->ticket;
-      if (t >= ca.count) break;
+      if (t >= count) break;
       const int lp = ca.order[t];
       const int m = a.m[lp], n = a.n[lp];
       const double* A = a.A + a.offA[lp];
@@ -1765,7 +2265,7 @@ struct Solver {
           a.status[lp] = kUndef;
           a.obj[lp] = 0.0;
           if (a.pivots) a.pivots[lp] = -1;
-          if (a.info) a.info[lp] = 0;
+          if (a.info) a.info[lp] = a.info_or;
         }
         __syncthreads();
         continue;
@@ -1776,145 +2276,142 @@ struct Solver {
       load(g, c0, lc, A, b, c, A32);
       int pivots = 0, degen = 0, cur = 0, st, info = 0;
       const float* w = a.weight ? a.weight + a.offw[lp] : nullptr;
+      // final bases verified (and reported) in FP64: the FP32 tableau, and the
+      // FP64 one with steepest-edge pricing in plans (LU scratch); the FP64
+      // Dantzig path is the reference's method, reported as the oracle does
+      const bool verify = kFP32 || (ca.se && a.pricing == 1 && lu != nullptr);
       bool bland = false;
       // pivot count at the last FP64 refresh: its x_B and objective are
       // reported only if no pivot followed it (-1: none yet)
       int piv_fresh = -1;
-      const int max_piv = a.max_pivots > 0 ? a.max_pivots : 50 * (m + n) + 1000;
+      // FP32 plans with an FP64 pass stop an FP32 solve at 4 (m + n) + 200
+      // pivots (several times what these solves take) and hand the LP over
+      const int user_piv = a.max_pivots > 0 ? a.max_pivots : 50 * (m + n) + 1000;
+      const int max_piv = (kFP32 && a.fb) ? min(user_piv, 4 * (m + n) + 200) : user_piv;
       const T ptol = (T)a.ptol, opt_tol = (T)a.opt_tol;
-      if (na > 0) {
-        objective_row(g, c0, lc, c, true);
-        __syncthreads();
-        st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
-        if (CLUSTER) csync();
-        if (st == kOpt) {
-          const double z = (double)tab[(size_t)m * g.ldw + g.cw];
-          if (z < -a.phase1_tol) st = kNoFeas;
-        } else if (st == kUnbnd) {
-          st = kUndef;
-        }
-        if (st == kOpt) {
-          drive_out(g, c0, lc, a, pivots, cur);
-          objective_row(g, c0, lc, c, false);
-          __syncthreads();
+      // A solve whose final basis the FP64 check cannot verify is repeated
+      // cold from the slack basis when it was warm-started, with a pivot
+      // budget of its own; a cold one is reported BLPG_UNDEF.  Phase-I LPs
+      // (hints ignored) are verified when the plan has LU scratch: the
+      // refactorisation handles their negated rows.
+      const bool check = verify && (na == 0 || lu != nullptr);
+      int budget = max_piv;
+      for (int attempt = 0; attempt < 2; ++attempt) {
+        st = -1;
+        const bool warm = attempt == 0 && a.hint && na == 0;
+        if (attempt > 0) {
+          info |= kInfoFallback;
+          if (CLUSTER) csync();
+          load(g, c0, lc, A, b, c, A32);
+          piv_fresh = -1;
           bland = false;
           degen = 0;
-          st = primal(g, c0, lc, a, w, max_piv, pivots, bland, degen, cur);
+          budget = pivots + max_piv;
         }
-      } else {
-        // FP32: a solve whose final basis the FP64 refresh cannot verify is
-        // repeated cold from the slack basis when it was warm-started, with
-        // a pivot budget of its own; a cold one is reported BLPG_UNDEF.
-        int budget = max_piv;
-        for (int attempt = 0; attempt < 2; ++attempt) {
-          st = -1;
-          const bool warm = attempt == 0 && a.hint;
-          if (attempt > 0) {
-            info |= kInfoFallback;
-            if (CLUSTER) csync();
-            load(g, c0, lc, A, b, c, A32);
-            piv_fresh = -1;
+        if (na > 0) {
+          // phase I on the artificials' objective, drive-out, phase II
+          objective_row(g, c0, lc, c, true);
+          __syncthreads();
+          st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
+          if (CLUSTER) csync();
+          if (st == kOpt) {
+            const double z = (double)tab[(size_t)m * g.ldw + g.cw];
+            if (z < -a.phase1_tol) st = kNoFeas;
+          } else if (st == kUnbnd) {
+            st = kUndef;
+          }
+          if (st == kOpt) {
+            drive_out(g, c0, lc, a, pivots, cur);
+            objective_row(g, c0, lc, c, false);
+            __syncthreads();
             bland = false;
             degen = 0;
-            budget = pivots + max_piv;
+            st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
           }
-          if (warm) {
-            info |= kInfoWarm;
-            if (crash(g, c0, a.hint + a.offbasis[lp], a, pivots, cur, lc) > 0)
-              info |= kInfoPartial;
-            // feasibility of the crashed basis judged on the tableau itself
-            // (the final FP64 refresh verifies whatever basis the finish ends on)
-            const int fl = check_feasible(g, c0, lc, ptol, opt_tol);
-            if (fl & 1) {
-              st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
-            } else if (fl & 2) {
-              info |= kInfoDual;
-              st = dual_loop(g, c0, lc, a, budget, pivots, cur, ptol);
-              if (st == kOpt) st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
-            } else if (a.warm_mode == 1) {
-              // infeasible both ways: shift the costs of the columns with
-              // d_j < -opt_tol to small distinct positive values (dual
-              // feasible), dual simplex to a primal-feasible basis, restore
-              // the true costs, primal simplex
-              info |= kInfoDual | kInfoShift;
-              T* drow = tab + (size_t)m * g.ldw;
-              for (int lj = tid; lj < lc; lj += nt) {
-                const int j = cvar[c0 + lj];
-                if (j < n + m && drow[lj] < -opt_tol)
-                  drow[lj] = (T)a.shift * (T(1) + (T)((j * 7919) % 1000) / T(1000));
-              }
-              __syncthreads();
-              st = dual_loop(g, c0, lc, a, budget, pivots, cur, ptol);
-              if (st == kOpt) {
-                objective_row(g, c0, lc, c, false);
-                __syncthreads();
+        } else {
+            if (warm) {
+              info |= kInfoWarm;
+              if (crash(g, c0, a.hint + a.offbasis[lp], a, pivots, cur, lc) > 0)
+                info |= kInfoPartial;
+              // feasibility of the crashed basis judged on the tableau itself
+              // (the final FP64 refresh verifies whatever basis the finish ends on)
+              const int fl = check_feasible(g, c0, lc, ptol, opt_tol);
+              if (fl & 1) {
                 st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
+              } else if (fl & 2) {
+                info |= kInfoDual;
+                st = dual_loop(g, c0, lc, a, budget, pivots, cur, ptol);
+                if (st == kOpt) st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
+              } else if (a.warm_mode == 1) {
+                // infeasible both ways: shift the costs of the columns with
+                // d_j < -opt_tol to small distinct positive values (dual
+                // feasible), dual simplex to a primal-feasible basis, restore
+                // the true costs, primal simplex
+                info |= kInfoDual | kInfoShift;
+                T* drow = tab + (size_t)m * g.ldw;
+                for (int lj = tid; lj < lc; lj += nt) {
+                  const int j = cvar[c0 + lj];
+                  if (j < n + m && drow[lj] < -opt_tol)
+                    drow[lj] = (T)a.shift * (T(1) + (T)((j * 7919) % 1000) / T(1000));
+                }
+                __syncthreads();
+                st = dual_loop(g, c0, lc, a, budget, pivots, cur, ptol);
+                if (st == kOpt) {
+                  objective_row(g, c0, lc, c, false);
+                  __syncthreads();
+                  st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
+                }
+              }
+              if (st < 0 || st == kNoFeas) {
+                // infeasible both ways (or dual simplex stuck): cold solve
+                info |= kInfoFallback;
+                if (CLUSTER) csync();
+                load(g, c0, lc, A, b, c, A32);
+                piv_fresh = -1;
+                bland = false;
+                degen = 0;
+                st = -1;
               }
             }
-            if (st < 0 || st == kNoFeas) {
-              // infeasible both ways (or dual simplex stuck): cold solve
-              info |= kInfoFallback;
-              if (CLUSTER) csync();
-              load(g, c0, lc, A, b, c, A32);
-              piv_fresh = -1;
-              bland = false;
-              degen = 0;
-              st = -1;
-            }
-          }
           if (st < 0) {
             const int period = kFP32 ? a.refresh_period : 0;
             for (;;) {
               st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur, period);
               if (st != kRefresh) break;
               if (CLUSTER) csync();
-              refresh(g, A, b, c, a);
+              if (refresh(g, A, b, c, a) & 8) info |= kInfoFactor;
               piv_fresh = pivots;
               info |= kInfoRefresh;
             }
           }
-          // FP32: verify the final basis in FP64 and repair if needed (at
-          // most four repairs, each verified by another refresh)
-          if (kFP32 && st == kOpt) {
-            bool verified = false;
-            for (int round = 0; round <= 4; ++round) {
-              if (CLUSTER) csync();
-              const int fl = refresh(g, A, b, c, a);
-              piv_fresh = pivots;
-              info |= kInfoRefresh;
-              if (!(fl & 4)) break;  // refinement did not converge
-              if ((fl & 3) == 3) {
-                verified = true;
-                break;
-              }
-              if (round == 4) break;
-              info |= kInfoRepair;
-              if (!(fl & 1)) {
-                info |= kInfoDual;
-                st = dual_loop(g, c0, lc, a, budget, pivots, cur, ptol);
-                if (st != kOpt) break;
-              }
-              st = primal(g, c0, lc, a, w, budget, pivots, bland, degen, cur);
-              if (st != kOpt) break;
-            }
-            if (st == kOpt && !verified) st = kUnverified;
-          }
-          // a warm start that ends unverified or at the pivot cap: once more, cold
-          if (kFP32 && warm && (st == kUnverified || st == kUndef)) continue;
-          break;
         }
-        if (st == kUnverified) {
-          st = kUndef;
-          info |= kInfoUnverified;
-        }
-        // FP32 unbounded: x_B of the final basis (where unboundedness was
-        // found) from the FP64 refresh too, not from the FP32 tableau
-        if (kFP32 && st == kUnbnd && piv_fresh != pivots) {
-          if (CLUSTER) csync();
-          refresh(g, A, b, c, a);
-          piv_fresh = pivots;
-          info |= kInfoRefresh;
-        }
+        // verify the final basis in FP64 and repair it if needed
+        if (check && st == kOpt)
+          st = verify_basis(g, c0, lc, A, b, c, a, w, budget, pivots, bland, degen, cur,
+                            piv_fresh, info);
+        // a warm start that ends unverified or at the pivot cap: once more, cold
+        if (check && warm && (st == kUnverified || st == kUndef)) continue;
+        break;
+      }
+      if (st == kUnverified) {
+        st = kUndef;
+        info |= kInfoUnverified;
+      }
+      // unbounded: x_B of the final basis (where unboundedness was found)
+      // from the FP64 refresh too, not from the FP32 tableau
+      if (check && st == kUnbnd && piv_fresh != pivots) {
+        if (CLUSTER) csync();
+        if (refresh(g, A, b, c, a) & 8) info |= kInfoFactor;
+        piv_fresh = pivots;
+        info |= kInfoRefresh;
+      }
+      // FP32 plans: an LP the FP32 tableau could not settle (unverified, at
+      // the pivot cap, or "infeasible" although b >= 0 makes the origin
+      // feasible) goes to the plan's FP64 pass, which overwrites its results
+      if (kFP32 && a.fb && (st == kUndef || (na == 0 && st == kNoFeas)) && rank == 0 &&
+          tid == 0) {
+        const int k = atomicAdd(a.fb, 1);
+        a.fb[1 + k] = lp;
       }
       const bool refreshed = piv_fresh == pivots;
       if (CLUSTER) csync();
@@ -1925,7 +2422,7 @@ struct Solver {
           a.status[lp] = st;
           a.obj[lp] = refreshed ? sh->z : (double)tab[(size_t)m * g.ldw + g.cw];
           if (a.pivots) a.pivots[lp] = pivots;
-          if (a.info) a.info[lp] = info;
+          if (a.info) a.info[lp] = info | a.info_or;
         }
         if (a.basis)
           for (int i = tid; i < m; i += nt) a.basis[a.offbasis[lp] + i] = basis[i];
@@ -1958,7 +2455,8 @@ struct Solver {
 };
 
 template <typename T, bool CLUSTER>
-__global__ void __launch_bounds__(512, 1) solve_kernel(const LpArgs a, const ClassArgs ca) {
+__global__ void __launch_bounds__(512, 1) solve_kernel(const __grid_constant__ LpArgs a,
+                                                        const __grid_constant__ ClassArgs ca) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Solver<T, CLUSTER> s;
   const Layout L(0, 0, 0, (int)sizeof(T), ca.se);  // the fixed header
@@ -1969,6 +2467,7 @@ __global__ void __launch_bounds__(512, 1) solve_kernel(const LpArgs a, const Cla
   s.sh = reinterpret_cast<SharedState*>(smem_raw + L.state);
   s.K = ca.K;
   s.rank = CLUSTER ? (int)cg::this_cluster().block_rank() : 0;
+  s.lu = ca.lu ? ca.lu + (size_t)(blockIdx.x / ca.K) * (size_t)ca.lu_stride : nullptr;
   s.run(a, ca);
 }
 

@@ -57,7 +57,7 @@ def test_full_config(built, kind):
     for pricing in ("dantzig", "steepest"):
         g = sp.solve(batch, "fp32", pricing=pricing)
         assert np.array_equal(g.status, cpu.status), pricing
-        assert (g.info[opt] & 16).all(), pricing  # every optimum verified by the FP64 refresh
+        assert (g.info[opt] & (16 | 1024)).all(), pricing  # verified in FP64, or re-solved in FP64
         assert _rel(g.objective[opt], cpu.objective[opt]).max() <= FP32_REL, pricing
 
 
@@ -121,3 +121,28 @@ def test_netlib_other_modes(built, known_golden, prec, pricing, tol):
         ex = v["exact_objective"]
         assert abs(g.objective[k] - ex) <= tol * max(1.0, abs(ex)), (nm, prec, pricing,
                                                                      g.objective[k], ex)
+
+
+def test_fp64_pass_of_fp32_plans(built, known_golden):
+    """LPs the FP32 tableau cannot settle (Netlib's BLEND, ADLITTLE, SC205 in
+    some pricing modes: unverified, stalled at the FP32 pivot cap) are handed
+    to the plan's FP64 pass, which solves them from scratch with the FP64
+    Dantzig method: their results are bit for bit the FP64 solve's, flagged
+    BLPG_INFO_FP64.  A pivot cap the FP64 pass shares leaves them UNDEF."""
+    names, batch = _netlib(known_golden)
+    f64 = sp.solve(batch, "fp64", want_x=True)
+    handed = 0
+    for pricing in ("dantzig", "steepest"):
+        g = sp.solve(batch, "fp32", pricing=pricing, want_x=True)
+        fb = (g.info & 1024) != 0
+        handed += int(fb.sum())
+        _, _, oc = batch.offsets()
+        for k in np.nonzero(fb)[0]:
+            assert g.status[k] == f64.status[k] and g.pivots[k] == f64.pivots[k], names[k]
+            assert g.objective[k] == f64.objective[k], names[k]
+            sl = slice(int(oc[k]), int(oc[k] + batch.n[k]))
+            assert np.array_equal(g.x[sl], f64.x[sl]), names[k]
+    assert handed > 0
+    capped = sp.solve(batch, "fp32", max_pivots=5)
+    assert (capped.status == 1).all() and (capped.pivots == 5).all()
+    assert ((capped.info & 1024) != 0).all()

@@ -5,9 +5,12 @@ blpg_solve_noalloc serves callers that cannot call cudaMalloc (code running
 inside a memory pool it does not own, or a framework that has handed all
 device memory to its own allocator): it takes only caller-provided device
 buffers and keeps its work-queue scratch in a fixed array inside the library.
-It runs the same pivot kernel with the same rules, so its results must be
-bit-identical to blpg_solve_batch's (the FP64 tolerance of the parity tests)
-and, in FP32, equal to the FP32 path's.  Two calls in a row check that the
+It runs the same pivot kernel with the same rules, so FP64 results are
+bit-identical to blpg_solve_batch's.  In FP32 they are bit-identical on every
+LP that blpg_solve_batch verified by iterative refinement alone; where a plan
+factorised a basis in FP64 (BLPG_INFO_FACTOR: its LU scratch is plan
+memory, which this entry point does not have) the allocation-free call
+reports the same status or BLPG_UNDEF.  Two calls in a row check that the
 shared scratch is reset between calls.  This file is collected last.
 """
 import ctypes as C
@@ -56,12 +59,27 @@ def _call(batch, d, precision, max_m=None, max_n=None):
             d["x"].cpu().numpy())
 
 
-def _same(got, want, call=None):
+FACTOR = 512 | 256  # BLPG_INFO_FACTOR | BLPG_INFO_REINVERT
+
+
+def _same(got, want, call=None, batch=None):
+    """Bit-identical results, except (FP32 plans) on LPs the plan verified by
+    an FP64 factorisation: there the same status or BLPG_UNDEF."""
     st, obj, piv, x = got
-    assert np.array_equal(st, want.status), call
-    assert np.array_equal(piv, want.pivots), call
-    assert np.array_equal(obj.view(np.uint64), want.objective.view(np.uint64)), call
-    assert np.array_equal(x.view(np.uint64), want.x.view(np.uint64)), call
+    plain = np.ones(st.size, bool) if want.info is None else (want.info & FACTOR) == 0
+    assert plain.mean() > 0.9, call
+    assert np.array_equal(st[plain], want.status[plain]), call
+    assert np.array_equal(piv[plain], want.pivots[plain]), call
+    assert np.array_equal(obj[plain].view(np.uint64), want.objective[plain].view(np.uint64)), call
+    if batch is not None:
+        _, _, oc = batch.offsets()
+        for k in np.nonzero(plain)[0]:
+            sl = slice(int(oc[k]), int(oc[k] + batch.n[k]))
+            assert np.array_equal(x[sl].view(np.uint64), want.x[sl].view(np.uint64)), (call, k)
+    else:
+        assert np.array_equal(x.view(np.uint64), want.x.view(np.uint64)), call
+    rest = ~plain
+    assert ((st[rest] == want.status[rest]) | (st[rest] == 1)).all(), call
 
 
 @pytest.mark.parametrize("kind,count", [(1, 400), (4, 160)])
@@ -77,7 +95,7 @@ def test_noalloc_matches_solve_batch(built, kind, count, precision, name):
     for call in range(2):
         d["status"].fill_(-9)
         d["obj"].fill_(float("nan"))
-        _same(_call(batch, d, precision), want, call)
+        _same(_call(batch, d, precision), want, call, batch)
     if precision == 0:  # and the FP64 oracle's, bit for bit
         _same(_call(batch, d, precision), oracle.solve_batch(batch, "fp64", want_x=True))
 
@@ -88,7 +106,7 @@ def test_noalloc_large_tableaux_use_clusters(built, precision, name):
     batch = sp.generate(2, 24, seed=99)
     want = sp.solve(batch, name, want_x=True)
     d = _device(batch)
-    _same(_call(batch, d, precision), want)
+    _same(_call(batch, d, precision), want, batch=batch)
 
 
 @pytest.mark.parametrize("precision", [0, 1])
@@ -110,8 +128,10 @@ def test_noalloc_refuses_phase_one_and_oversized_lps(built, precision):
     assert st[6] == 1 and piv[6] == -1
     assert st[7] == 1 and piv[7] == -1
     want = sp.solve(base, "fp32" if precision else "fp64")
-    assert np.array_equal(st[:6], want.status) and np.array_equal(piv[:6], want.pivots)
-    assert np.array_equal(obj[:6].view(np.uint64), want.objective.view(np.uint64))
+    plain = (want.info & FACTOR) == 0
+    assert np.array_equal(st[:6][plain], want.status[plain])
+    assert np.array_equal(piv[:6][plain], want.pivots[plain])
+    assert np.array_equal(obj[:6][plain].view(np.uint64), want.objective[plain].view(np.uint64))
 
 
 def test_noalloc_rejects_oversized_batches(built):
