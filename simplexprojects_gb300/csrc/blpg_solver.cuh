@@ -1256,9 +1256,9 @@ struct Solver {
   // in a fixed order, independent of the thread count and the cluster split.
   // Returns the bits of refresh_refine.  Out of line with the geometry by
   // value: it runs once or twice per LP.
-  __device__ __noinline__ int refresh_lu(const Geom g, const double* A, const double* b,
-                                         const double* c, const double opt_tol,
-                                         const double ptol) {
+  __device__ __forceinline__ int refresh_lu_body(const Geom g, const double* A,
+                                                 const double* b, const double* c,
+                                                 const double opt_tol, const double ptol) {
     const int m = g.m, n = g.n, na = g.na;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
@@ -1588,6 +1588,36 @@ struct Solver {
     __syncwarp();
   }
 
+  // Out-of-line entries of the rarely run FP64 refreshes and the rebuild.
+  // They are static and take a copy of the solver (its shared-memory
+  // pointers), so that no member function's `this` escapes and the kernel
+  // keeps every pointer of its hot loops in registers.
+  static __device__ __noinline__ int refresh_lu_call(Solver self, const Geom g, const double* A,
+                                                     const double* b, const double* c,
+                                                     const double opt_tol, const double ptol) {
+    return self.refresh_lu_body(g, A, b, c, opt_tol, ptol);
+  }
+  static __device__ __noinline__ int refresh_refine_call(Solver self, const Geom g,
+                                                         const double* A, const double* b,
+                                                         const double* c, const double opt_tol,
+                                                         const double ptol) {
+    return self.refresh_refine_body(g, A, b, c, opt_tol, ptol);
+  }
+  static __device__ __noinline__ void reinvert_call(Solver self, const Geom g, const double* A) {
+    self.reinvert_body(g, A);
+  }
+  __device__ __forceinline__ int refresh_lu(const Geom& g, const double* A, const double* b,
+                                            const double* c, double opt_tol, double ptol) {
+    return refresh_lu_call(*this, g, A, b, c, opt_tol, ptol);
+  }
+  __device__ __forceinline__ int refresh_refine(const Geom& g, const double* A, const double* b,
+                                                const double* c, double opt_tol, double ptol) {
+    return refresh_refine_call(*this, g, A, b, c, opt_tol, ptol);
+  }
+  __device__ __forceinline__ void reinvert(const Geom& g, const double* A) {
+    reinvert_call(*this, g, A);
+  }
+
   // The FP64 refresh: iterative refinement through the tableau's B^-1 (the
   // fast path, FP64 work proportional to the structural basics), or, with LU
   // scratch (plans; the allocation-free entry point has none), the
@@ -1613,7 +1643,7 @@ struct Solver {
   // solves, entries rounded to the tableau's type; the RHS and the objective
   // row were set by refresh_lu.  Used before repair pivots, when the tableau
   // has drifted too far from its basis for the repairs to be trusted.
-  __device__ __noinline__ void reinvert(const Geom g, const double* A) {
+  __device__ __forceinline__ void reinvert_body(const Geom g, const double* A) {
     const int m = g.m, n = g.n;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
@@ -1683,9 +1713,9 @@ struct Solver {
   // dot product per nonbasic structural column.  Returns bit 0: x_B >= -ptol,
   // bit 1: d >= -opt_tol (both judged in FP64), bit 2: both refinements
   // converged (without it bits 0 and 1 prove nothing).  Single-phase LPs only.
-  __device__ __noinline__ int refresh_refine(const Geom g, const double* A, const double* b,
-                                             const double* c, const double opt_tol,
-                                             const double ptol) {
+  __device__ __forceinline__ int refresh_refine_body(const Geom g, const double* A,
+                                                     const double* b, const double* c,
+                                                     const double opt_tol, const double ptol) {
     const int m = g.m, n = g.n;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
@@ -1811,11 +1841,14 @@ struct Solver {
         const int sv = vpos[n + k];
         yr[k] = sv >= 0 ? (double)*elem(g, m, sv) : 0.0;
       }
-      // the k range of each structural basic's column sum is split in P
-      // parts (partial sums in `part`, 192 doubles), combined in a fixed
-      // order; P = 1 above 96 basics
+      // y_k is exactly 0 for every basic slack k (it starts at 0 and its
+      // correction is its own residual, -y_k), so the sums over k below run
+      // over the nonbasic slacks (nlist, nn of them) only.  The range of each
+      // structural basic's column sum is split in P parts (partial sums in
+      // `part`, 192 doubles), combined in a fixed order; P = 1 above 96
+      // basics
       const int P = (ns > 0 && ns <= 96) ? min(4, 192 / ns) : 1;
-      const int kc = ceil_div(m, P);
+      const int kc = ceil_div(nn, P);
       bool yconv = false;
       for (int it = 0; it < kRefineIters; ++it) {
         if (tid == 0) mx[0] = mx[1] = 0u;
@@ -1825,14 +1858,15 @@ struct Solver {
         for (int w = tid; w < ns * P; w += nt) {
           const int t = w % ns, pp = w / ns;
           const int col = basis[slist[t]];
-          const int k0 = pp * kc, k1 = min(m, k0 + kc);
+          const int u0 = pp * kc, u1 = min(nn, u0 + kc);
           double p0 = 0.0, p1 = 0.0;
-          int k = k0;
-          for (; k + 2 <= k1; k += 2) {
+          int u = u0;
+          for (; u + 2 <= u1; u += 2) {
+            const int k = nlist[u], k2 = nlist[u + 1];
             p0 = fma(__ldg(A + (size_t)k * n + col), yr[k], p0);
-            p1 = fma(__ldg(A + (size_t)(k + 1) * n + col), yr[k + 1], p1);
+            p1 = fma(__ldg(A + (size_t)k2 * n + col), yr[k2], p1);
           }
-          if (k < k1) p0 = fma(__ldg(A + (size_t)k * n + col), yr[k], p0);
+          if (u < u1) p0 = fma(__ldg(A + (size_t)nlist[u] * n + col), yr[nlist[u]], p0);
           if (P == 1) {
             const double sv = c[col] - (p0 + p1);
             res[slist[t]] = sv;
@@ -1896,21 +1930,23 @@ struct Solver {
         __syncthreads();
       }
       // Reduced costs d_j = y^T a_j - c_j of the nonbasic structural
-      // columns: one thread per column over coalesced rows of A, four
-      // interleaved partial sums.  Nonbasic slack k: d = y_k.
+      // columns: one thread per column over coalesced rows of A (the rows of
+      // the nonbasic slacks: y is 0 on the others), four interleaved partial
+      // sums.  Nonbasic slack k: d = y_k.
       bool badd = false, badp = false;
       for (int j = tid; j < n; j += nt) {
         const int sv = vpos[j];
         if (sv < 0) continue;
         double p0 = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;
-        int k = 0;
-        for (; k + 4 <= m; k += 4) {
-          p0 = fma(__ldg(A + (size_t)k * n + j), yr[k], p0);
-          p1 = fma(__ldg(A + (size_t)(k + 1) * n + j), yr[k + 1], p1);
-          p2 = fma(__ldg(A + (size_t)(k + 2) * n + j), yr[k + 2], p2);
-          p3 = fma(__ldg(A + (size_t)(k + 3) * n + j), yr[k + 3], p3);
+        int u = 0;
+        for (; u + 4 <= nn; u += 4) {
+          const int k0 = nlist[u], k1 = nlist[u + 1], k2 = nlist[u + 2], k3 = nlist[u + 3];
+          p0 = fma(__ldg(A + (size_t)k0 * n + j), yr[k0], p0);
+          p1 = fma(__ldg(A + (size_t)k1 * n + j), yr[k1], p1);
+          p2 = fma(__ldg(A + (size_t)k2 * n + j), yr[k2], p2);
+          p3 = fma(__ldg(A + (size_t)k3 * n + j), yr[k3], p3);
         }
-        for (; k < m; ++k) p0 = fma(__ldg(A + (size_t)k * n + j), yr[k], p0);
+        for (; u < nn; ++u) p0 = fma(__ldg(A + (size_t)nlist[u] * n + j), yr[nlist[u]], p0);
         const double d = ((p0 + p1) + (p2 + p3)) - c[j];
         *elem(g, m, sv) = (T)d;
         badd = badd || d < -opt_tol;
