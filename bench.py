@@ -14,8 +14,10 @@ on).  One step = one solve of the whole workload batch.
 
   value        LPs/s with A, b, c already resident in HBM (plan replay; each
                step re-solves from the input data, nothing is cached)
-  e2e          LPs/s through the public C ABI (blpg_solve_batch) from host
-               buffers: host->device copy of A, b, c and device->host copy of
+  e2e          LPs/s through the public C ABI from host buffers
+               (blpg_learned_solve for the learned warm start of workload 3,
+               blpg_solve_batch for the others): host->device copy of A, b, c
+               (and the family ids) and device->host copy of
                status/objective/pivots inside the timed region
   roofline     algorithmic bytes per pivot of the condensed tableau
                s * (2 (m+1) W + 4 (m+1)), W = n + 1 stored columns (nonbasic
@@ -289,7 +291,7 @@ def run_learned(args, rank, world, local, dist=None):
     ms_solve = max_over_ranks(statistics.median(t_solve))
     ok = pres.status == 5
     rel = np.abs(res.objective[ok] - pres.objective[ok]) / np.maximum(np.abs(pres.objective[ok]), 1.0)
-    # e2e through the public call from host arrays (pinned)
+    # e2e through the public C ABI call (blpg_learned_solve) from host arrays (pinned)
     evalp = pinned(evalb)
     e2e = []
     for i in range(args.warmup + args.steps):
@@ -312,7 +314,7 @@ def run_learned(args, rank, world, local, dist=None):
     flops = float((piv * 2.0 * (m + 1) * (n + 1)).sum())
     ach_tf = flops / (ms_solve * 1e-3) / 1e12
     cpu = None if args.no_cpu_baseline else cpu_baseline(evalb, "fp64")
-    h2d = int(evalb.A.nbytes + evalb.b.nbytes + evalb.c.nbytes)
+    h2d = int(evalb.A.nbytes + evalb.b.nbytes + evalb.c.nbytes + 4 * evalb.count)
     total = 10_000
     out = {
         "metric": "LPs/s", "value": total / (ms * 1e-3), "unit": "LPs/s", "n_gpus": world,
@@ -348,7 +350,8 @@ def run_learned(args, rank, world, local, dist=None):
         "status_match": float((res.status == pres.status).mean()),
         "max_rel_obj_err_vs_fp64": float(rel.max()) if rel.size else 0.0,
         "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "LPs/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": int(total * 16), "ms_per_step": e2e_ms},
+                "d2h_bytes_per_step": int(total * 16), "ms_per_step": e2e_ms,
+                "call": "blpg_learned_solve (include/blpg.h)"},
         "roofline": {"bound": "smem", "achieved": ach, "peak": smem.value, "unit": "GB/s",
                      "frac": ach / smem.value, "traffic": None,
                      "kernel": "solve_kernel<float> (FP32 condensed tableau pivots)",

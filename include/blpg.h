@@ -181,9 +181,16 @@ enum {
                                 its basis: before repair pivots when an FP64 check kept
                                 failing, or once in a long or degenerate FP32 solve
                                 (plans only) */
-  BLPG_INFO_FACTOR = 512     /* an FP64 refresh factorised the basis (LU) instead of
+  BLPG_INFO_FACTOR = 512,    /* an FP64 refresh factorised the basis (LU) instead of
                                 refining through the tableau's B^-1: every phase-I LP,
                                 and bases the refinement could not settle (plans only) */
+  BLPG_INFO_FP64 = 1024,     /* FP32 plans: the FP32 tableau could not settle this LP
+                                (unverified, at its pivot cap 4 (m + n) + 200, or
+                                "infeasible" with b >= 0); the plan's FP64 pass solved it
+                                from scratch with the FP64 Dantzig method */
+  BLPG_INFO_RETRY = 2048     /* a warm-started solve ended on a basis the FP64 check could
+                                not verify and was re-run cold from the slack basis (one that
+                                hits the pivot cap is re-run too, with BLPG_INFO_FALLBACK) */
 };
 
 /* Fill *opt with the defaults above. */
@@ -196,6 +203,20 @@ void blpg_options_init(blpg_options* opt);
  * anywhere in an LP switches that LP to phase I; simplex.cu:574-583). */
 int32_t blpg_solve_batch(const blpg_batch* batch, const blpg_options* opt,
                          blpg_result* out);
+/* A packed batch (null offset arrays) whose uploads reach 64 MB is solved in
+ * eight chunks of LPs with about equal A volume, each with its own plan and
+ * stream; the uploads run one chunk after another on one stream, so that
+ * each chunk's uploads overlap the previous chunks' solves (simplex.cu:914-955
+ * overlaps its copies over N streams the same way).  One
+ * whose inputs and outputs exceed half the device's free memory is solved in
+ * as many chunks as that budget needs, taking turns in two device regions
+ * (the reference's tester splits such batches by device memory on the host,
+ * GPU_Tester.cu:194-238).  Results are the same as one plan's.  Tuning-table
+ * keys "overlap_mb" and "device_budget_mb" change the two thresholds and
+ * "overlap_chunks" the chunk count.
+ * blpg_solve_batch_chunks returns how many chunks the last call used
+ * (1: one plan). */
+int32_t blpg_solve_batch_chunks(void);
 
 /* Plans: the size classes, work queues, device scratch and CUDA graph for
  * one batch shape, built once and replayed.  blpg_plan_create reads only the
@@ -235,16 +256,26 @@ int32_t blpg_plan_class_info(const blpg_plan* plan, int32_t cls,
  * persistent grid (CTAs) it is launched with. */
 int32_t blpg_plan_class_residency(const blpg_plan* plan, int32_t cls,
                                   int32_t* ctas_per_sm, int32_t* grid);
+/* Tuning key of size class `cls` (the CTAs per SM its layout admits for a
+ * single-CTA class, 100 + K for a class of K-CTA clusters: the "fpXX_cC"
+ * entries of blpg_set_tuning) and, when lp_ids is non-null, the ids of its
+ * LPs (num_lps of them, blpg_plan_class_info), in the order it solves them. */
+int32_t blpg_plan_class_key(const blpg_plan* plan, int32_t cls, int32_t* key,
+                            int32_t* lp_ids);
 /* Kernel launches one blpg_plan_execute performs. */
 int32_t blpg_plan_launches(const blpg_plan* plan);
 void blpg_plan_destroy(blpg_plan* plan);
 
-/* Size-class table (JSON text, as written by the autotuner): overrides the
- * built-in heuristic for threads per CTA ("fp64_k1": 256, per precision and
- * cluster size), the per-CTA shared-memory budget ("fp32_smem": bytes) and
- * the cap on CTAs per SM for single-CTA LPs ("fp32_ctas": 2; default: as
- * many as shared memory admits, at most 16 in FP32 and 4 in FP64).  Null
- * resets. */
+/* Size-class table (JSON text, as written by the autotuner,
+ * simplexprojects_gb300/autotune.py): threads per CTA per precision and
+ * cluster size ("fp64_k1": 256), per size class ("fp32_c2": 224, the class
+ * key of blpg_plan_class_key) with the CTAs per SM it runs with
+ * ("fp32_c2_ctas": 2), the per-CTA shared-memory budget ("fp32_smem": bytes)
+ * and the cap on CTAs per SM of single-CTA classes ("fp32_ctas": 2; default:
+ * as many as shared memory admits, at most 16 in FP32 and 4 in FP64).  The
+ * library starts from the table tuned on GB300 that the build compiles in
+ * (simplexprojects_gb300/tuning/gb300.json); a table given here replaces it,
+ * a null table restores it.  Later plans and blpg_solve_batch calls use it. */
 int32_t blpg_set_tuning(const char* json_text);
 
 const char* blpg_last_error(void);
@@ -347,6 +378,27 @@ int32_t blpg_price_weights(const float* d_scores, int32_t lds, int32_t count,
 int32_t blpg_topm_hint(const float* d_scores, int32_t lds, int32_t count,
                        const int32_t* d_m, const int32_t* d_n, int32_t max_cols,
                        const int64_t* d_offhint, int32_t* d_hint, void* stream);
+
+/* The learned warm start end to end, for a batch of LPs of one shape (no
+ * reference counterpart).  blpg_learned_create takes a trained network
+ * (blpg_mlp, not owned: it must outlive the solver), the feature statistics
+ * of its training set (HOST arrays, families x (n + m): per family the mean
+ * and the standard deviation of each of c_1..c_n, b_1..b_m), the guidance
+ * strength beta (weights 1 + beta * p_j) and the batch's shapes and offsets
+ * (A, b, c may be null); it builds an FP32 steepest-edge plan (the options'
+ * precision and tolerances are kept, pricing is set to steepest edge) and
+ * the device buffers.  blpg_learned_solve then takes HOST arrays of that
+ * batch (same shapes and offsets) and the family id of each LP, uploads
+ * them, runs features -> network -> weights -> solve on one stream and
+ * downloads status, objective and (when non-null) x, pivots and info;
+ * synchronous.  Pinned host arrays upload fastest. */
+typedef struct blpg_learned blpg_learned;
+int32_t blpg_learned_create(blpg_mlp* mlp, int32_t families, const float* host_mean,
+                            const float* host_std, float beta, const blpg_batch* shapes,
+                            const blpg_options* opt, blpg_learned** out);
+int32_t blpg_learned_solve(blpg_learned* solver, const blpg_batch* host_batch,
+                           const int32_t* host_family, blpg_result* host_out);
+void blpg_learned_destroy(blpg_learned* solver);
 
 /* ---------------------------------------------------------------------------
  * Reference batch files and synthetic workloads (host only, no GPU needed).

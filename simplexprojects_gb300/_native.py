@@ -54,6 +54,7 @@ class Result(C.Structure):
 SIGNATURES = {
     "blpg_options_init": (None, [C.POINTER(Options)]),
     "blpg_solve_batch": (C.c_int32, [C.POINTER(Batch), C.POINTER(Options), C.POINTER(Result)]),
+    "blpg_solve_batch_chunks": (C.c_int32, []),
     "blpg_plan_create": (C.c_int32, [C.POINTER(Batch), C.POINTER(Options), C.POINTER(C.c_void_p)]),
     "blpg_plan_execute": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.POINTER(Result), C.c_void_p]),
@@ -66,6 +67,7 @@ SIGNATURES = {
     "blpg_plan_class_info": (C.c_int32, [C.c_void_p, C.c_int32, i32p, i32p, i32p, i32p]),
     "blpg_plan_class_residency": (C.c_int32, [C.c_void_p, C.c_int32, i32p, i32p]),
     "blpg_plan_launches": (C.c_int32, [C.c_void_p]),
+    "blpg_plan_class_key": (C.c_int32, [C.c_void_p, C.c_int32, i32p, i32p]),
     "blpg_plan_destroy": (None, [C.c_void_p]),
     "blpg_set_tuning": (C.c_int32, [C.c_char_p]),
     "blpg_last_error": (C.c_char_p, []),
@@ -87,6 +89,12 @@ SIGNATURES = {
     "blpg_mlp_gradients": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                        C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "blpg_features": (C.c_int32, [C.c_int32] * 4 + [C.c_void_p] * 8 + [C.c_int32, C.c_void_p]),
+    "blpg_learned_create": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_float),
+                                        C.POINTER(C.c_float), C.c_float, C.POINTER(Batch),
+                                        C.POINTER(Options), C.POINTER(C.c_void_p)]),
+    "blpg_learned_solve": (C.c_int32, [C.c_void_p, C.POINTER(Batch), C.POINTER(C.c_int32),
+                                       C.POINTER(Result)]),
+    "blpg_learned_destroy": (None, [C.c_void_p]),
     "blpg_topm_hint": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                    C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "blpg_read_abc": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, i32p, i32p, f64p, f64p, f64p]),

@@ -11,6 +11,10 @@ Host code is compiled with ``-ffp-contract=off`` (the workload generator must
 give bit-identical data on x86 and Arm) and the solver's device code with
 ``--fmad=false`` (every fused multiply-add in it is an explicit ``fma``, as in
 the oracle).
+
+The size-class table tuned on GB300 (``tuning/gb300.json``, written by
+``autotune.py``) is compiled into the library as its default table
+(``_build/blpg_tuning_default.inc``).
 """
 from __future__ import annotations
 
@@ -30,6 +34,8 @@ LIB = LIBDIR / "libblpg.so"
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_BUILD = ORACLE_DIR / "_build"
 ORACLE_LIB = ORACLE_BUILD / "libblpg_oracle.so"
+TUNING = PKG / "tuning" / "gb300.json"
+TUNING_INC = BUILD / "blpg_tuning_default.inc"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -47,6 +53,7 @@ SOURCES = [
     ("blpg_peaks.cu", []),
     ("blpg_noalloc.cu", ["--fmad=false"]),
     ("blpg_mlp.cu", []),
+    ("blpg_learned.cu", []),
     ("blpg_gen.cpp", []),
 ]
 
@@ -55,14 +62,30 @@ def _common(nvcc: str) -> list[str]:
     return [
         nvcc, "-std=c++17", "-O3", *ARCH, "-lineinfo",
         "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
-        "-I", str(ROOT / "include"),
+        "-I", str(ROOT / "include"), "-I", str(BUILD),
     ]
+
+
+def _tuning_include() -> Path:
+    """The compiled-in default tuning table: tuning/gb300.json as a C string
+    (an empty table when the file is absent); rewritten only on change."""
+    import json
+    text = "{}"
+    if TUNING.exists():
+        table = json.loads(TUNING.read_text())
+        text = json.dumps({k: v for k, v in table.items() if isinstance(v, int)})
+    body = ("// generated by build.py from tuning/gb300.json\n"
+            f'static const char kDefaultTuning[] = R"BLPGJSON({text})BLPGJSON";\n')
+    if not TUNING_INC.exists() or TUNING_INC.read_text() != body:
+        TUNING_INC.write_text(body)
+    return TUNING_INC
 
 
 def _compile(nvcc: str, src: str, extra: list[str]) -> Path:
     obj = BUILD / (Path(src).stem + ".o")
     srcp = CSRC / src
-    deps = [srcp, *CSRC.glob("*.h"), *CSRC.glob("*.cuh"), ROOT / "include" / "blpg.h"]
+    deps = [srcp, *CSRC.glob("*.h"), *CSRC.glob("*.cuh"), ROOT / "include" / "blpg.h",
+            TUNING_INC]
     if obj.exists() and obj.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
         return obj
     cmd = _common(nvcc) + extra + ["-c", str(srcp), "-o", str(obj)]
@@ -80,6 +103,7 @@ def build_library(verbose: bool = False) -> Path:
     nvcc = _nvcc()
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(exist_ok=True)
+    _tuning_include()
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(SOURCES), os.cpu_count() or 1))) as ex:
         objs = list(ex.map(lambda s: _compile(nvcc, s[0], s[1]), SOURCES))
     if LIB.exists() and LIB.stat().st_mtime >= max(o.stat().st_mtime for o in objs):

@@ -1,0 +1,208 @@
+// The learned warm start behind the C ABI (blpg_learned_*): one call takes a
+// host batch of LPs of one shape, uploads A, b, c and the family ids, forms
+// the network's features, runs the network, turns its basis probabilities
+// into steepest-edge score weights and solves the batch with an FP32 plan,
+// then downloads the results.  No reference counterpart (the reference has
+// no learned part); it replaces the steps a caller of the plan API would
+// otherwise chain by hand (blpg_features, blpg_mlp_predict,
+// blpg_price_weights, blpg_plan_execute_weighted).
+//
+// Everything is enqueued on one stream in that order; host arrays in pinned
+// memory make the uploads and downloads asynchronous to the host until the
+// final synchronisation.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "blpg_internal.h"
+
+struct blpg_learned {
+  blpg_mlp* mlp = nullptr;  // not owned
+  blpg_plan* plan = nullptr;
+  int count = 0, m = 0, n = 0, families = 0;
+  float beta = 1.f;
+  int d_in_pad = 0, d_out_pad = 0, rows = 0;
+  int64_t extA = 0, extb = 0, extc = 0, extw = 0;
+  cudaStream_t stream = nullptr;
+  // device buffers
+  double *A = nullptr, *b = nullptr, *c = nullptr, *obj = nullptr, *x = nullptr;
+  int32_t *fam = nullptr, *dm = nullptr, *dn = nullptr, *st = nullptr, *piv = nullptr,
+          *info = nullptr;
+  int64_t *offb = nullptr, *offc = nullptr, *offw = nullptr;
+  float *mean = nullptr, *std_ = nullptr, *X = nullptr, *logits = nullptr, *w = nullptr;
+};
+
+namespace {
+
+#define LCK(call)                                                                           \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return blpg::fail(e_ == cudaErrorMemoryAllocation ? BLPG_ENOMEM : BLPG_ECUDA,         \
+                        "blpg_learned: %s: %s", #call, cudaGetErrorString(e_));             \
+  } while (0)
+
+void release(blpg_learned* L) {
+  if (!L) return;
+  if (L->plan) blpg_plan_destroy(L->plan);
+  void* bufs[] = {L->A, L->b, L->c, L->obj, L->x, L->fam, L->dm, L->dn, L->st, L->piv, L->info,
+                  L->offb, L->offc, L->offw, L->mean, L->std_, L->X, L->logits, L->w};
+  for (void* p : bufs) cudaFree(p);
+  if (L->stream) cudaStreamDestroy(L->stream);
+}
+
+}  // namespace
+
+extern "C" int32_t blpg_learned_create(blpg_mlp* mlp, int32_t families, const float* host_mean,
+                                       const float* host_std, float beta,
+                                       const blpg_batch* shapes, const blpg_options* opt_in,
+                                       blpg_learned** out) {
+  using blpg::fail;
+  if (!mlp || !host_mean || !host_std || !shapes || !out || families < 1 || shapes->count < 1 ||
+      !shapes->m || !shapes->n)
+    return fail(BLPG_EINVAL, "blpg_learned_create: null or empty argument");
+  *out = nullptr;
+  const int N = shapes->count, m = shapes->m[0], n = shapes->n[0];
+  for (int k = 0; k < N; ++k)
+    if (shapes->m[k] != m || shapes->n[k] != n)
+      return fail(BLPG_EINVAL, "blpg_learned_create: LP %d is %dx%d, the batch's shape is %dx%d",
+                  k, shapes->m[k], shapes->n[k], m, n);
+  int32_t din = 0, dout = 0;
+  int32_t rc = blpg_mlp_dims(mlp, &din, &dout);
+  if (rc) return rc;
+  if (din < n + m + families || dout < n + m)
+    return fail(BLPG_EINVAL,
+                "blpg_learned_create: the network reads %d features and scores %d columns; "
+                "the batch needs %d and %d",
+                din, dout, n + m + families, n + m);
+  blpg_options opt;
+  if (opt_in)
+    opt = *opt_in;
+  else
+    blpg_options_init(&opt);
+  opt.pricing = BLPG_PRICE_STEEPEST;  // the network's probabilities weight steepest edge
+  opt.basis_hint = nullptr;
+  opt.price_weight = nullptr;
+  blpg_learned* L = new blpg_learned;
+  L->mlp = mlp;
+  L->count = N;
+  L->m = m;
+  L->n = n;
+  L->families = families;
+  L->beta = beta;
+  L->d_in_pad = din;
+  L->d_out_pad = dout;
+  L->rows = (N + 63) / 64 * 64;
+  auto bail = [&](int32_t code) {
+    release(L);
+    delete L;
+    return code;
+  };
+  if ((rc = blpg_plan_create(shapes, &opt, &L->plan))) return bail(rc);
+  // offsets as the plan reads them (packed when null), and the weights' packing
+  std::vector<int64_t> ob(N), oc(N), ow(N);
+  int64_t pa = 0, pb = 0, pc = 0;
+  for (int k = 0; k < N; ++k) {
+    const int64_t oa = shapes->off_A ? shapes->off_A[k] : pa;
+    ob[k] = shapes->off_b ? shapes->off_b[k] : pb;
+    oc[k] = shapes->off_c ? shapes->off_c[k] : pc;
+    ow[k] = (int64_t)k * (n + m);
+    L->extA = std::max(L->extA, oa + (int64_t)m * n);
+    L->extb = std::max(L->extb, ob[k] + m);
+    L->extc = std::max(L->extc, oc[k] + n);
+    pa += (int64_t)m * n;
+    pb += m;
+    pc += n;
+  }
+  L->extw = (int64_t)N * (n + m);
+  cudaError_t e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(fail(BLPG_ECUDA, "blpg_learned_create: stream"));
+  const size_t F = (size_t)families * (n + m);
+#define LMAL(p, bytes)                                                              \
+  do {                                                                              \
+    if (cudaMalloc(&(p), (bytes)) != cudaSuccess)                                   \
+      return bail(fail(BLPG_ENOMEM, "blpg_learned_create: %zu bytes", (size_t)(bytes))); \
+  } while (0)
+  LMAL(L->A, sizeof(double) * (size_t)L->extA);
+  LMAL(L->b, sizeof(double) * (size_t)L->extb);
+  LMAL(L->c, sizeof(double) * (size_t)L->extc);
+  LMAL(L->obj, sizeof(double) * N);
+  LMAL(L->x, sizeof(double) * (size_t)L->extc);
+  LMAL(L->fam, sizeof(int32_t) * N);
+  LMAL(L->dm, sizeof(int32_t) * N);
+  LMAL(L->dn, sizeof(int32_t) * N);
+  LMAL(L->st, sizeof(int32_t) * N);
+  LMAL(L->piv, sizeof(int32_t) * N);
+  LMAL(L->info, sizeof(int32_t) * N);
+  LMAL(L->offb, sizeof(int64_t) * N);
+  LMAL(L->offc, sizeof(int64_t) * N);
+  LMAL(L->offw, sizeof(int64_t) * N);
+  LMAL(L->mean, sizeof(float) * F);
+  LMAL(L->std_, sizeof(float) * F);
+  LMAL(L->X, sizeof(float) * (size_t)L->rows * din);
+  LMAL(L->logits, sizeof(float) * (size_t)L->rows * dout);
+  LMAL(L->w, sizeof(float) * (size_t)L->extw);
+#undef LMAL
+  std::vector<int32_t> mm(N, m), nn(N, n);
+  cudaMemcpy(L->dm, mm.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice);
+  cudaMemcpy(L->dn, nn.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice);
+  cudaMemcpy(L->offb, ob.data(), sizeof(int64_t) * N, cudaMemcpyHostToDevice);
+  cudaMemcpy(L->offc, oc.data(), sizeof(int64_t) * N, cudaMemcpyHostToDevice);
+  cudaMemcpy(L->offw, ow.data(), sizeof(int64_t) * N, cudaMemcpyHostToDevice);
+  cudaMemcpy(L->mean, host_mean, sizeof(float) * F, cudaMemcpyHostToDevice);
+  cudaMemcpy(L->std_, host_std, sizeof(float) * F, cudaMemcpyHostToDevice);
+  // feature rows past the batch stay zero
+  cudaMemset(L->X, 0, sizeof(float) * (size_t)L->rows * din);
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess)
+    return bail(fail(BLPG_ECUDA, "blpg_learned_create: %s", cudaGetErrorString(e)));
+  *out = L;
+  return BLPG_OK;
+}
+
+extern "C" int32_t blpg_learned_solve(blpg_learned* L, const blpg_batch* bt,
+                                      const int32_t* host_family, blpg_result* out) {
+  using blpg::fail;
+  if (!L || !bt || !host_family || !out || !out->status || !out->objective)
+    return fail(BLPG_EINVAL, "blpg_learned_solve: null argument");
+  if (bt->count != L->count || !bt->A || !bt->b || !bt->c)
+    return fail(BLPG_EINVAL, "blpg_learned_solve: the batch is not the one the solver was made for");
+  const int N = L->count;
+  cudaStream_t s = L->stream;
+  LCK(cudaMemcpyAsync(L->A, bt->A, sizeof(double) * (size_t)L->extA, cudaMemcpyHostToDevice, s));
+  LCK(cudaMemcpyAsync(L->b, bt->b, sizeof(double) * (size_t)L->extb, cudaMemcpyHostToDevice, s));
+  LCK(cudaMemcpyAsync(L->c, bt->c, sizeof(double) * (size_t)L->extc, cudaMemcpyHostToDevice, s));
+  LCK(cudaMemcpyAsync(L->fam, host_family, sizeof(int32_t) * N, cudaMemcpyHostToDevice, s));
+  int32_t rc;
+  if ((rc = blpg_features(N, L->m, L->n, L->families, L->offb, L->offc, L->b, L->c, L->fam,
+                          L->mean, L->std_, L->X, L->d_in_pad, s)))
+    return rc;
+  if ((rc = blpg_mlp_predict(L->mlp, L->X, L->rows, L->logits, s))) return rc;
+  if ((rc = blpg_price_weights(L->logits, L->d_out_pad, N, L->dm, L->dn, L->n + L->m, L->offw,
+                               L->beta, L->w, s)))
+    return rc;
+  blpg_result dres{L->st, L->obj, out->x ? L->x : nullptr, out->pivots ? L->piv : nullptr,
+                   nullptr, out->info ? L->info : nullptr};
+  if ((rc = blpg_plan_execute_weighted(L->plan, L->A, L->b, L->c, nullptr, L->w, &dres, s)))
+    return rc;
+  LCK(cudaMemcpyAsync(out->status, L->st, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, s));
+  LCK(cudaMemcpyAsync(out->objective, L->obj, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+  if (out->x)
+    LCK(cudaMemcpyAsync(out->x, L->x, sizeof(double) * (size_t)L->extc, cudaMemcpyDeviceToHost,
+                        s));
+  if (out->pivots)
+    LCK(cudaMemcpyAsync(out->pivots, L->piv, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, s));
+  if (out->info)
+    LCK(cudaMemcpyAsync(out->info, L->info, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, s));
+  LCK(cudaStreamSynchronize(s));
+  return BLPG_OK;
+}
+
+extern "C" void blpg_learned_destroy(blpg_learned* L) {
+  if (!L) return;
+  if (L->stream) cudaStreamSynchronize(L->stream);
+  release(L);
+  delete L;
+}

@@ -99,6 +99,7 @@ constexpr int kInfoUnverified = 128;  // FP32: the FP64 refresh could not verify
 constexpr int kInfoReinvert = 256;    // the tableau was rebuilt from an FP64 factorisation
 constexpr int kInfoFactor = 512;      // an FP64 refresh used the LU factorisation (refresh_lu)
 constexpr int kInfoFp64 = 1024;       // re-solved on an FP64 tableau (the FP64 pass of an FP32 plan)
+constexpr int kInfoRetry = 2048;      // a warm start ended unverified or at the pivot cap: re-run cold
 
 struct ClassArgs {
   const int32_t* order;  // LP ids of this class, heaviest first
@@ -2426,7 +2427,10 @@ struct Solver {
           st = verify_basis(g, c0, lc, A, b, c, a, w, budget, pivots, bland, degen, cur,
                             piv_fresh, info);
         // a warm start that ends unverified or at the pivot cap: once more, cold
-        if (check && warm && (st == kUnverified || st == kUndef)) continue;
+        if (check && warm && (st == kUnverified || st == kUndef)) {
+          if (st == kUnverified) info |= kInfoRetry;
+          continue;
+        }
         break;
       }
       if (st == kUnverified) {

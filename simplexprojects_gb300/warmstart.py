@@ -298,7 +298,8 @@ class LearnedSolver:
     ``run()`` enqueues features -> network -> weights or hint -> solve on
     device-resident data (the plan's CUDA graph for the solve);
     ``solve(batch)`` is the end-to-end call from host arrays (copies of A, b,
-    c in, status / objective / pivots out)."""
+    c in, status / objective / pivots out): in guided mode one call of the C
+    ABI's blpg_learned_solve, which runs the same kernels in the same order."""
 
     def __init__(self, ws: WarmStart, batch: LPBatch, precision: str = "fp32",
                  mode: str = "guided", beta: float = 1.0, **opts):
@@ -328,6 +329,9 @@ class LearnedSolver:
         self.hint = torch.empty(int(batch.m.sum()), dtype=torch.int32, device=ws.dev)
         self.weight = torch.empty(int(nm.sum()), dtype=torch.float32, device=ws.dev)
         rows = (k + 63) // 64 * 64
+        self.opts = opts
+        self.precision = precision
+        self._cl = None  # the C ABI's blpg_learned, made at the first solve()
         self.scratch = dict(
             X=torch.zeros((rows, ws.mlp.d_in_pad), dtype=torch.float32, device=ws.dev),
             logits=torch.empty((rows, ws.mlp.d_out_pad), dtype=torch.float32, device=ws.dev))
@@ -356,9 +360,54 @@ class LearnedSolver:
     def result(self):
         return self.db.result()
 
-    def solve(self, batch: LPBatch):
+    def _learned(self):
+        """The C ABI's learned solver (blpg_learned) for this batch's shape."""
+        if self._cl is None:
+            from .solver import options
+            mean = np.ascontiguousarray(self.ws.mean.cpu().numpy(), dtype=np.float32)
+            std = np.ascontiguousarray(self.ws.std.cpu().numpy(), dtype=np.float32)
+            o = options(self.precision, **self.opts)
+            bst = self.batch.c_struct()
+            h = C.c_void_p()
+            N.check(N.lib().blpg_learned_create(
+                self.ws.mlp.h, self.ws.F, mean.ctypes.data_as(C.POINTER(C.c_float)),
+                std.ctypes.data_as(C.POINTER(C.c_float)), float(self.beta), C.byref(bst),
+                C.byref(o), C.byref(h)), "blpg_learned_create")
+            self._cl = h
+        return self._cl
+
+    def close(self):
+        if self._cl is not None:
+            N.lib().blpg_learned_destroy(self._cl)
+            self._cl = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, batch: LPBatch, want_x: bool = False):
         """End to end from host arrays (same shapes and offsets as at
-        construction): upload A, b, c, predict, solve, download results."""
+        construction): upload A, b, c, predict, solve, download results.
+        Guided mode: one call of blpg_learned_solve (the C ABI)."""
+        if self.mode == "guided":
+            from .solver import SolveResult
+            h = self._learned()
+            k = batch.count
+            st = np.zeros(k, np.int32)
+            ob = np.zeros(k, np.float64)
+            pv = np.zeros(k, np.int32)
+            info = np.zeros(k, np.int32)
+            _, _, oc = batch.offsets()
+            x = np.zeros(int((oc + batch.n).max())) if want_x else None
+            res = N.Result(N.ptr(st, C.c_int32), N.ptr(ob, C.c_double), N.ptr(x, C.c_double),
+                           N.ptr(pv, C.c_int32), None, N.ptr(info, C.c_int32))
+            fam = np.ascontiguousarray(batch.family, dtype=np.int32)
+            bst = batch.c_struct()
+            N.check(N.lib().blpg_learned_solve(h, C.byref(bst), N.ptr(fam, C.c_int32),
+                                               C.byref(res)), "blpg_learned_solve")
+            return SolveResult(st, ob, pv, x, None, info)
         torch = self.torch
         # asynchronous when the host arrays are pinned (stream-ordered before
         # the solve; result() synchronises)

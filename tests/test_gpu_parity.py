@@ -277,3 +277,8 @@ def test_fp32_shared_A_copy_phase_one(built):
         assert np.array_equal(a.objective, p.objective)
         assert np.array_equal(a.x, p.x)
         assert np.array_equal(a.status, c64.status)
+        # every phase-I optimum verified in FP64 by the factorised refresh
+        # (or re-solved by the plan's FP64 pass): objectives within 1e-6
+        opt = c64.status == 5
+        assert (a.info[opt] & (16 | 1024)).all(), pricing
+        assert _rel(a.objective[opt], c64.objective[opt]).max() <= FP32_REL, pricing
