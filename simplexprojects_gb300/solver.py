@@ -114,8 +114,10 @@ class Plan:
             per_sm, grid = C.c_int32(), C.c_int32()
             N.check(self._L.blpg_plan_class_residency(self._h, i, C.byref(per_sm), C.byref(grid)),
                     "class_residency")
+            key = C.c_int32()
+            N.check(self._L.blpg_plan_class_key(self._h, i, C.byref(key), None), "class_key")
             out.append(dict(cluster=K.value, threads=nt.value, smem=sm.value, lps=cnt.value,
-                            ctas_per_sm=per_sm.value, grid=grid.value))
+                            ctas_per_sm=per_sm.value, grid=grid.value, key=key.value))
         return out
 
     def launches(self) -> int:
