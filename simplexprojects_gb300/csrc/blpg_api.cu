@@ -19,6 +19,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <atomic>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -55,13 +56,26 @@ using dev::Geom;
 using dev::Layout;
 using dev::LpArgs;
 
-// Tuning overrides (autotuner JSON): per (precision, K) a threads-per-CTA.
+// Tuning table (autotuner JSON).  Keys per precision p (fp64 | fp32):
+//   "p_kK"        threads per CTA of cluster classes of K CTAs (K = 1: the
+//                 default of every single-CTA class)
+//   "p_cC"        threads per CTA of size class C (C = the CTAs per SM its
+//                 layout admits for a single-CTA class, 100 + K for a cluster
+//                 class); "p_cC_ctas" the CTAs per SM it runs with (at most C)
+//   "p_smem"      the per-CTA shared-memory budget that picks cluster sizes
+//   "p_ctas"      the cap on CTAs per SM of every single-CTA class
+// The library starts from the table tuned on GB300 that the build compiles
+// in (tuning/gb300.json); blpg_set_tuning replaces it, and a null table
+// restores it.
 struct Tuning {
   std::mutex mu;
-  std::map<std::pair<int, int>, int> threads;  // (precision*16 + K, size bucket)
+  std::map<std::pair<int, int>, int> threads;  // (precision*16 + field, class or bucket)
   int generation = 0;  // bumped by every blpg_set_tuning: cached plans are rebuilt
+  bool loaded = false;
 };
 static Tuning g_tuning;
+#include "blpg_tuning_default.inc"  // kDefaultTuning: the compiled-in table (JSON text)
+static void parse_tuning_locked(const char* json);
 
 static int device_check(int device, cudaDeviceProp* prop) {
   int ndev = 0;
@@ -79,6 +93,7 @@ static int device_check(int device, cudaDeviceProp* prop) {
 
 struct ClassPlan {
   int K = 1, nt = 128, max_m = 0, max_na = 0, smem = 0;
+  int key = 1;  // tuning key: CTAs per SM the layout admits (single CTA), 100 + K (clusters)
   int max_ns = 0;  // most structural basics any member can have: min(m, n)
   long long lu_off = 0, lu_stride = 0;  // the class's LU refresh scratch (doubles)
   int ctas_per_sm = 1;
@@ -194,6 +209,10 @@ static int kernel_regs(bool cluster) {
 
 static int tuning_value(int key0, int key1, int dflt) {
   std::lock_guard<std::mutex> lk(g_tuning.mu);
+  if (!g_tuning.loaded) {
+    parse_tuning_locked(kDefaultTuning);
+    g_tuning.loaded = true;
+  }
   auto it = g_tuning.threads.find({key0, key1});
   return it != g_tuning.threads.end() ? it->second : dflt;
 }
@@ -204,17 +223,19 @@ static int tuning_value(int key0, int key1, int dflt) {
 // most threads -- whole rows of lanes, at most the tuning table's threads
 // per CTA (default 512) -- whose registers keep that many CTAs resident.
 // Fewer CTAs per SM when a row of lanes does not fit otherwise.
-static int pick_threads(const blpg_plan* p, int nl, int smem, int regs, int K, int override_nt,
-                        int* ctas_out) {
+static int pick_threads(const blpg_plan* p, int nl, int smem, int regs, int K, int key,
+                        int override_nt, int* ctas_out) {
   const int by_smem = std::max(1, p->smem_per_sm / (smem + p->smem_reserved));
-  int target = tuning_value(p->precision * 16 + 14, 2, 0);
+  int target = tuning_value(p->precision * 16 + 12, 1000 + key, 0);  // this class's
+  if (target <= 0) target = tuning_value(p->precision * 16 + 14, 2, 0);  // every class's
   target = target > 0 ? std::min(target, by_smem) : by_smem;
   const int regs_alloc = dev::round_up(std::max(regs, 1), 8);
   if (override_nt > 0) {  // explicit threads per CTA: residency follows from it
     *ctas_out = 0;
     return std::min(dev::round_up(std::max(override_nt, nl), 32), kMaxThreads);
   }
-  const int want = tuning_value(p->precision * 16 + K, 0, 512);
+  int want = tuning_value(p->precision * 16 + 13, 1000 + key, 0);  // this class's
+  if (want <= 0) want = tuning_value(p->precision * 16 + K, 0, 512);
   for (int ctas = target; ctas >= 1; --ctas) {
     int cap = std::min(kMaxThreads, (p->regs_per_sm / ctas) / (regs_alloc * 32) * 32);
     cap = std::min(cap, p->threads_per_sm / ctas / 32 * 32);
@@ -303,6 +324,7 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
                      [&](int a, int b) { return items[a].work > items[b].work; });
     ClassPlan c;
     c.K = kv.first < 100 ? 1 : kv.first - 100;
+    c.key = kv.first;
     int nl = 1;
     for (int lp : lps) {
       c.smem = std::max(c.smem, items[lp].bytes);
@@ -313,8 +335,8 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
       nl = std::max(nl, items[lp].nl);
     }
     // threads: every member's row of vector lanes at least once
-    c.nt = pick_threads(p, nl, c.smem, kernel_regs<T>(c.K > 1), c.K, p->opt.threads_per_cta,
-                        &c.ctas_per_sm);
+    c.nt = pick_threads(p, nl, c.smem, kernel_regs<T>(c.K > 1), c.K, c.key,
+                        p->opt.threads_per_cta, &c.ctas_per_sm);
     c.count = (int)lps.size();
     int per_sm = 0, clusters = 0;
     int rc = occupancy<T>(c, &per_sm, &clusters);
@@ -533,14 +555,10 @@ extern "C" const char* blpg_version(void) {
   return "blpg-gb300 1.0 (sm_103a; abi 1)";
 }
 
-extern "C" int32_t blpg_set_tuning(const char* json) {
-  std::lock_guard<std::mutex> lk(g_tuning.mu);
+namespace blpg {
+static void parse_tuning_locked(const char* json) {
   g_tuning.threads.clear();
-  ++g_tuning.generation;
-  if (!json) return BLPG_OK;
-  // Minimal reader for {"fp64_k1": 256, "fp32_k2": 512, "fp64_smem": 115712,
-  // "fp32_ctas": 2, ...}: threads per CTA per (precision, cluster size), the
-  // CTA smem budget and the CTAs per SM target.
+  if (!json) return;
   const char* s = json;
   while ((s = std::strchr(s, '"'))) {
     const char* e = std::strchr(s + 1, '"');
@@ -548,17 +566,47 @@ extern "C" int32_t blpg_set_tuning(const char* json) {
     std::string key(s + 1, e - s - 1);
     const char* colon = std::strchr(e, ':');
     if (!colon) break;
-    int val = std::atoi(colon + 1);
-    int prec = -1, K = 0;
-    if (std::sscanf(key.c_str(), "fp64_k%d", &K) == 1) prec = BLPG_FP64;
-    else if (std::sscanf(key.c_str(), "fp32_k%d", &K) == 1) prec = BLPG_FP32;
-    if (prec >= 0 && val > 0 && val <= 1024) g_tuning.threads[{prec * 16 + K, 0}] = val;
-    if (key == "fp64_smem" && val > 0) g_tuning.threads[{BLPG_FP64 * 16 + 15, 1}] = val;
-    if (key == "fp32_smem" && val > 0) g_tuning.threads[{BLPG_FP32 * 16 + 15, 1}] = val;
-    if (key == "fp64_ctas" && val > 0) g_tuning.threads[{BLPG_FP64 * 16 + 14, 2}] = val;
-    if (key == "fp32_ctas" && val > 0) g_tuning.threads[{BLPG_FP32 * 16 + 14, 2}] = val;
+    const char* v = colon + 1;
+    while (*v == ' ' || *v == '\n' || *v == '\t') ++v;
+    if (*v == '{' || *v == '[') {  // nested data ("measured"): skip the key
+      s = e + 1;
+      continue;
+    }
+    const int val = std::atoi(v);
+    int bits = 0, K = 0, cls = 0;
+    char tail[16] = {0};
+    int prec = -1;
+    if (std::sscanf(key.c_str(), "fp%d_", &bits) == 1) prec = bits == 64 ? BLPG_FP64 : (bits == 32 ? BLPG_FP32 : -1);
+    if (prec >= 0) {
+      const char* rest = key.c_str() + 5;
+      if (std::sscanf(rest, "k%d%15s", &K, tail) == 1 && val > 0 && val <= 1024)
+        g_tuning.threads[{prec * 16 + K, 0}] = val;
+      else if (std::sscanf(rest, "c%d%15s", &cls, tail) == 2 && std::strcmp(tail, "_ctas") == 0 &&
+               val > 0)
+        g_tuning.threads[{prec * 16 + 12, 1000 + cls}] = val;
+      else if (std::sscanf(rest, "c%d%15s", &cls, tail) == 1 && val > 0 && val <= 1024)
+        g_tuning.threads[{prec * 16 + 13, 1000 + cls}] = val;
+      else if (std::strcmp(rest, "smem") == 0 && val > 0)
+        g_tuning.threads[{prec * 16 + 15, 1}] = val;
+      else if (std::strcmp(rest, "ctas") == 0 && val > 0)
+        g_tuning.threads[{prec * 16 + 14, 2}] = val;
+    } else if (key == "overlap_mb" && val > 0) {
+      g_tuning.threads[{-1, 1}] = val;
+    } else if (key == "device_budget_mb" && val > 0) {
+      g_tuning.threads[{-1, 2}] = val;
+    } else if (key == "overlap_chunks" && val > 1) {
+      g_tuning.threads[{-1, 3}] = val;
+    }
     s = colon + 1;
   }
+}
+}  // namespace blpg
+
+extern "C" int32_t blpg_set_tuning(const char* json) {
+  std::lock_guard<std::mutex> lk(g_tuning.mu);
+  parse_tuning_locked(json ? json : kDefaultTuning);
+  g_tuning.loaded = true;
+  ++g_tuning.generation;
   return BLPG_OK;
 }
 
@@ -859,6 +907,17 @@ extern "C" int32_t blpg_plan_class_residency(const blpg_plan* p, int32_t cls,
   return BLPG_OK;
 }
 
+extern "C" int32_t blpg_plan_class_key(const blpg_plan* p, int32_t cls, int32_t* key,
+                                       int32_t* lp_ids) {
+  if (!p || cls < 0 || cls >= (int32_t)p->classes.size())
+    return fail(BLPG_EINVAL, "blpg_plan_class_key: bad plan or class");
+  const ClassPlan& c = p->classes[cls];
+  if (key) *key = c.key;
+  if (lp_ids) std::copy(p->order.begin() + c.order_off, p->order.begin() + c.order_off + c.count,
+                        lp_ids);
+  return BLPG_OK;
+}
+
 extern "C" int32_t blpg_plan_launches(const blpg_plan* p) {
   return p ? p->launches : fail(BLPG_EINVAL, "null plan");
 }
@@ -920,6 +979,273 @@ static bool plan_layout_matches(const Workspace& w, const blpg_batch* bt, const 
 }
 }  // namespace blpg
 
+// ---------------------------------------------------------------------------
+// Chunked host-buffer solve: a packed batch (no offset arrays) whose uploads
+// are large, or that does not fit the device's free memory, is split into
+// contiguous chunks of LPs with about equal A volume, each with its own plan
+// and stream.  Chunk k's uploads run on its stream while chunk k - 1 solves
+// (the reference overlaps its copies and kernels over N streams the same
+// way, simplex.cu:914-955), and its results come back as soon as it is done.
+// When the whole batch does not fit, chunks take turns in two device regions
+// (a chunk waits for the one two before it to finish with its region), which
+// replaces the reference's host-side split by device memory
+// (GPU_Tester.cu:194-238, 284-354).
+// ---------------------------------------------------------------------------
+namespace blpg {
+
+constexpr size_t kOverlapBytes = size_t(64) << 20;  // uploads above this are pipelined
+constexpr int kOverlapChunks = 8;  // measured best of 3, 4 and 8 for FP32 on GB300
+constexpr int kMaxChunks = 64;
+
+struct ChunkCache {
+  std::mutex mu;
+  int device = -1;
+  void* buf = nullptr;
+  size_t cap = 0;
+  std::vector<blpg_plan*> plans;
+  std::vector<cudaEvent_t> done;    // per region: its last chunk's downloads are enqueued
+  std::vector<cudaEvent_t> landed;  // per chunk: its uploads are enqueued
+  cudaStream_t up = nullptr;        // every chunk's uploads, in chunk order
+  std::vector<int32_t> bounds;    // LP index of each chunk's start, then count
+  std::vector<int32_t> key_shapes, key_negs;
+  blpg_options key_opt{};
+  int key_tuning = -1, ring = 0;
+  void clear() {
+    for (auto* pl : plans) blpg_plan_destroy(pl);
+    plans.clear();
+    for (auto e : done) cudaEventDestroy(e);
+    for (auto e : landed) cudaEventDestroy(e);
+    done.clear();
+    landed.clear();
+  }
+};
+static ChunkCache g_chunks;
+static std::atomic<int> g_last_chunks{0};  // chunks of the last blpg_solve_batch (1 = one plan)
+
+// Chunk bounds with about equal A volume, at least `per` LPs each.
+static std::vector<int32_t> chunk_bounds(const blpg_batch* bt, int chunks) {
+  const int N = bt->count;
+  int64_t total = 0;
+  for (int k = 0; k < N; ++k) total += (int64_t)bt->m[k] * bt->n[k];
+  std::vector<int32_t> bounds{0};
+  int64_t acc = 0;
+  for (int k = 0; k < N; ++k) {
+    acc += (int64_t)bt->m[k] * bt->n[k];
+    const int done_chunks = (int)bounds.size();
+    if (done_chunks < chunks && acc * chunks >= total * done_chunks && k + 1 < N)
+      bounds.push_back(k + 1);
+  }
+  bounds.push_back(N);
+  return bounds;
+}
+
+// Returns BLPG_OK after solving, or 1 when the batch is not for this path.
+static int32_t solve_chunked(const blpg_batch* bt, const blpg_options& opt, blpg_result* out,
+                             const std::vector<int32_t>& shapes) {
+  if (bt->off_A || bt->off_b || bt->off_c) return 1;
+  const int N = bt->count;
+  int64_t eA = 0, eb = 0, ec = 0;
+  for (int k = 0; k < N; ++k) {
+    eA += (int64_t)bt->m[k] * bt->n[k];
+    eb += bt->m[k];
+    ec += bt->n[k];
+  }
+  const size_t h2d = sizeof(double) * (size_t)(eA + eb + ec);
+  size_t free_b = 0, total_b = 0;
+  int ndev = 0;  // no usable device: the one-plan path reports it
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || opt.device < 0 || opt.device >= ndev) return 1;
+  CK(cudaSetDevice(opt.device));
+  CK(cudaMemGetInfo(&free_b, &total_b));
+  // inputs and outputs may take half the free memory (the plans' own state
+  // needs the rest); the tuning table's "device_budget_mb" lowers that and
+  // "overlap_mb" sets the upload volume from which copies are pipelined
+  size_t budget = free_b / 2;
+  const int budget_mb = tuning_value(-1, 2, 0);
+  if (budget_mb > 0) budget = std::min(budget, (size_t)budget_mb << 20);
+  const size_t io = h2d * 5 / 4;
+  const bool big = h2d >= ((size_t)tuning_value(-1, 1, (int)(kOverlapBytes >> 20)) << 20);
+  const bool tight = io > budget;
+  if (!big && !tight) return 1;
+  int chunks = std::max(2, std::min(kMaxChunks, tuning_value(-1, 3, kOverlapChunks)));
+  int ring = chunks;
+  if (tight) {  // two regions of at most half the budget each
+    ring = 2;
+    chunks = (int)std::min<size_t>(kMaxChunks, std::max<size_t>(kOverlapChunks,
+                                                                io / std::max<size_t>(1, budget / 2) + 1));
+  }
+  if (N < 2 * chunks) return 1;
+  const bool hint = opt.basis_hint != nullptr, wt = opt.price_weight != nullptr;
+  std::vector<int32_t> negs((size_t)N);
+  {
+    int64_t pb = 0;
+    for (int k = 0; k < N; ++k) {
+      int neg = 0;
+      for (int i = 0; i < bt->m[k]; ++i) neg += bt->b[pb + i] < 0.0 ? 1 : 0;
+      negs[k] = neg;
+      pb += bt->m[k];
+    }
+  }
+  std::lock_guard<std::mutex> lk(g_chunks.mu);
+  ChunkCache& cc = g_chunks;
+  const bool reuse = !cc.plans.empty() && cc.key_shapes == shapes && cc.key_negs == negs &&
+                     same_plan_options(cc.key_opt, opt) && cc.key_tuning == tuning_generation() &&
+                     cc.ring == ring && (int)cc.plans.size() == chunks;
+  // per-chunk prefix offsets (packed layout)
+  std::vector<int32_t> bounds = reuse ? cc.bounds : chunk_bounds(bt, chunks);
+  chunks = (int)bounds.size() - 1;
+  std::vector<int64_t> pA(N + 1, 0), pB(N + 1, 0), pC(N + 1, 0), pW(N + 1, 0);
+  for (int k = 0; k < N; ++k) {
+    pA[k + 1] = pA[k] + (int64_t)bt->m[k] * bt->n[k];
+    pB[k + 1] = pB[k] + bt->m[k];
+    pC[k + 1] = pC[k] + bt->n[k];
+    pW[k + 1] = pW[k] + bt->m[k] + bt->n[k];
+  }
+  if (!reuse) {
+    cc.clear();
+    cc.ring = std::min(ring, chunks);
+    for (int ch = 0; ch < chunks; ++ch) {
+      const int lo = bounds[ch], hi = bounds[ch + 1];
+      blpg_batch sub{hi - lo, bt->m + lo, bt->n + lo, nullptr, nullptr, nullptr,
+                     bt->A + pA[lo], bt->b + pB[lo], bt->c + pC[lo]};
+      blpg_plan* pl = nullptr;
+      int32_t rc = blpg_plan_create(&sub, &opt, &pl);
+      if (rc) {
+        cc.clear();
+        return rc;
+      }
+      cc.plans.push_back(pl);
+    }
+    for (int r = 0; r < cc.ring; ++r) {
+      cudaEvent_t e;
+      CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      cc.done.push_back(e);
+    }
+    for (int ch = 0; ch < chunks; ++ch) {
+      cudaEvent_t e;
+      CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      cc.landed.push_back(e);
+    }
+    if (cc.up) cudaStreamDestroy(cc.up);  // on the plans' device
+    cc.up = nullptr;
+    CK(cudaStreamCreateWithFlags(&cc.up, cudaStreamNonBlocking));
+    cc.bounds = bounds;
+    cc.key_shapes = shapes;
+    cc.key_negs = negs;
+    cc.key_opt = opt;
+    cc.key_tuning = tuning_generation();
+  }
+  // one region per ring slot, sized for the largest chunk
+  auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  size_t sA = 0, sb = 0, sc = 0, sn = 0, sw = 0;
+  for (int ch = 0; ch < chunks; ++ch) {
+    const int lo = bounds[ch], hi = bounds[ch + 1];
+    sA = std::max(sA, al(sizeof(double) * (size_t)(pA[hi] - pA[lo])));
+    sb = std::max(sb, al(sizeof(double) * (size_t)(pB[hi] - pB[lo])));
+    sc = std::max(sc, al(sizeof(double) * (size_t)(pC[hi] - pC[lo])));
+    sn = std::max(sn, al(sizeof(double) * (size_t)(hi - lo)));
+    sw = std::max(sw, al(sizeof(float) * (size_t)(pW[hi] - pW[lo])));
+  }
+  // A | b | c | status | objective | x | pivots | info | basis | hint | weights
+  const size_t region = sA + sb + sc + 4 * sn + sc + 2 * sb + sw;
+  const size_t need = region * (size_t)cc.ring;
+  if (cc.cap < need || cc.device != opt.device) {
+    for (auto* pl : cc.plans) cudaStreamSynchronize(pl->stream);
+    if (cc.buf) cudaFree(cc.buf);
+    cc.buf = nullptr;
+    cc.cap = 0;
+    CK(cudaMalloc(&cc.buf, need));
+    cc.cap = need;
+    cc.device = opt.device;
+  }
+  // Downloads into pageable host memory block the calling thread until the
+  // chunk is solved, so chunk j's downloads are enqueued only after the
+  // uploads and solve of chunk j + ring - 1 (the last chunk that can still
+  // start before chunk j's region is needed again).
+  std::vector<blpg_result> dres((size_t)chunks);
+  auto download = [&](int ch) -> int32_t {
+    blpg_plan* pl = cc.plans[ch];
+    cudaStream_t s = pl->stream;
+    const int lo = bounds[ch], hi = bounds[ch + 1], cn = hi - lo;
+    const blpg_result& d = dres[ch];
+    CK(cudaMemcpyAsync(out->status + lo, d.status, sizeof(int32_t) * cn, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out->objective + lo, d.objective, sizeof(double) * cn,
+                       cudaMemcpyDeviceToHost, s));
+    if (out->x)
+      CK(cudaMemcpyAsync(out->x + pC[lo], d.x, sizeof(double) * (size_t)(pC[hi] - pC[lo]),
+                         cudaMemcpyDeviceToHost, s));
+    if (out->pivots)
+      CK(cudaMemcpyAsync(out->pivots + lo, d.pivots, sizeof(int32_t) * cn, cudaMemcpyDeviceToHost,
+                         s));
+    if (out->info)
+      CK(cudaMemcpyAsync(out->info + lo, d.info, sizeof(int32_t) * cn, cudaMemcpyDeviceToHost, s));
+    if (out->basis)
+      CK(cudaMemcpyAsync(out->basis + pB[lo], d.basis,
+                         sizeof(int32_t) * (size_t)(pB[hi] - pB[lo]), cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(cc.done[ch % cc.ring], s));
+    return BLPG_OK;
+  };
+  int32_t rc = BLPG_OK;
+  for (int ch = 0; ch < chunks; ++ch) {
+    blpg_plan* pl = cc.plans[ch];
+    cudaStream_t s = pl->stream, u = cc.up;
+    const int r = ch % cc.ring;
+    // uploads go one chunk after another on one stream, so that each chunk
+    // lands at the full copy bandwidth (concurrent copies would share it and
+    // land together); a region is reused once its last chunk's downloads ran
+    if (ch >= cc.ring) CK(cudaStreamWaitEvent(u, cc.done[r], 0));
+    char* o = (char*)cc.buf + (size_t)r * region;
+    double* dA = (double*)o;
+    o += sA;
+    double* db = (double*)o;
+    o += sb;
+    double* dc = (double*)o;
+    o += sc;
+    const int lo = bounds[ch], hi = bounds[ch + 1];
+    blpg_result& d = dres[ch];
+    d = blpg_result{};
+    d.status = (int32_t*)o;
+    o += sn;
+    d.objective = (double*)o;
+    o += sn;
+    d.x = out->x ? (double*)o : nullptr;
+    o += sc;
+    d.pivots = out->pivots ? (int32_t*)o : nullptr;
+    o += sn;
+    d.info = out->info ? (int32_t*)o : nullptr;
+    o += sn;
+    d.basis = out->basis ? (int32_t*)o : nullptr;
+    int32_t* dhint = hint ? (int32_t*)(o + sb) : nullptr;
+    o += 2 * sb;
+    float* dw = wt ? (float*)o : nullptr;
+    CK(cudaMemcpyAsync(dA, bt->A + pA[lo], sizeof(double) * (size_t)(pA[hi] - pA[lo]),
+                       cudaMemcpyHostToDevice, u));
+    CK(cudaMemcpyAsync(db, bt->b + pB[lo], sizeof(double) * (size_t)(pB[hi] - pB[lo]),
+                       cudaMemcpyHostToDevice, u));
+    CK(cudaMemcpyAsync(dc, bt->c + pC[lo], sizeof(double) * (size_t)(pC[hi] - pC[lo]),
+                       cudaMemcpyHostToDevice, u));
+    if (hint)
+      CK(cudaMemcpyAsync(dhint, opt.basis_hint + pB[lo], sizeof(int32_t) * (size_t)(pB[hi] - pB[lo]),
+                         cudaMemcpyHostToDevice, u));
+    if (wt)
+      CK(cudaMemcpyAsync(dw, opt.price_weight + pW[lo], sizeof(float) * (size_t)(pW[hi] - pW[lo]),
+                         cudaMemcpyHostToDevice, u));
+    CK(cudaEventRecord(cc.landed[ch], u));
+    CK(cudaStreamWaitEvent(s, cc.landed[ch], 0));
+    if ((rc = blpg_plan_execute_weighted(pl, dA, db, dc, dhint, dw, &d, s))) return rc;
+    if (ch - (cc.ring - 1) >= 0 && (rc = download(ch - (cc.ring - 1)))) return rc;
+  }
+  for (int ch = std::max(0, chunks - cc.ring + 1); ch < chunks; ++ch)
+    if ((rc = download(ch))) return rc;
+  for (auto* pl : cc.plans) CK(cudaStreamSynchronize(pl->stream));
+  CK(cudaGetLastError());
+  g_last_chunks = chunks;
+  return BLPG_OK;
+}
+
+}  // namespace blpg
+
+extern "C" int32_t blpg_solve_batch_chunks(void) { return blpg::g_last_chunks.load(); }
+
 extern "C" int32_t blpg_solve_batch(const blpg_batch* bt, const blpg_options* opt_in,
                                     blpg_result* out) {
   if (!bt || !out || !out->status || !out->objective)
@@ -960,12 +1286,17 @@ extern "C" int32_t blpg_solve_batch(const blpg_batch* bt, const blpg_options* op
     return negs;
   };
 
-  std::lock_guard<std::mutex> lk(g_ws.mu);
-  int rc;
   const bool hint = opt.basis_hint != nullptr;
   const bool wt = opt.price_weight != nullptr;
   if (wt && opt.pricing != BLPG_PRICE_STEEPEST)
     return fail(BLPG_EINVAL, "blpg_solve_batch: pricing weights need steepest-edge pricing");
+  {
+    const int32_t rc0 = solve_chunked(bt, opt, out, shapes);
+    if (rc0 != 1) return rc0;  // solved in chunks (or failed there)
+  }
+  g_last_chunks = 1;
+  std::lock_guard<std::mutex> lk(g_ws.mu);
+  int rc;
   // workspace: A | b | c | status | obj | x | pivots | info | hint | weights
   // (256-byte aligned); its layout depends only on shapes and offsets
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
