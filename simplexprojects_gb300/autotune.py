@@ -3,25 +3,27 @@ size class of a plan, timed on the device class by class.
 
 A plan groups its LPs into size classes (single-CTA LPs by how many CTAs of
 their layout fit an SM, cluster LPs by cluster size K); every class has a
-tuning key (``blpg_plan_class_key``: that CTA count, or 100 + K).  For each
-class of a representative batch the tuner takes the class's LPs alone (a
-batch sharing the original arrays), times whole-batch plan replays (CUDA
-events) for candidate (threads per CTA, CTAs per SM), checks that statuses
-and objectives do not change, and keeps the fastest.  The result is the JSON
-table that ``blpg_set_tuning`` reads::
+tuning key (``blpg_plan_class_key``: that CTA count, or 100 + K).  The tuner
+takes, for each key, that class's LPs from every workload it is given, each
+repeated until they fill the GPU ``waves`` times over (a class of a few
+dozen LPs timed alone rewards wide CTAs that a full batch of them does not),
+times whole-batch plan replays (CUDA events) for candidate (threads per CTA,
+CTAs per SM), checks that statuses do not change, and keeps the candidate
+with the lowest sum over workloads of its time over that workload's best
+time.  The result is the JSON table that ``blpg_set_tuning`` reads::
 
     {"fp32_c2": 224, "fp32_c2_ctas": 2, "fp64_c104": 512, ...,
      "measured": {...}}
 
 The table tuned on GB300 for the benchmark workloads is committed as
 ``tuning/gb300.json`` and compiled into the library as its default table
-(``build.py``); ``load(path)`` applies another one, ``reset()`` restores the
-compiled-in one.
+(``build.py``); ``load(path)`` applies another one, ``override(entries)``
+lays entries over the compiled-in one and ``reset()`` restores it.
 
     python -m simplexprojects_gb300.autotune --out simplexprojects_gb300/tuning/gb300.json
 
-tunes FP32 steepest edge on workload 3 and FP32 / FP64 on workload 4 (every
-shape of the other workloads occurs there) and merges the three.
+tunes FP32 steepest edge on workloads 0-4 and FP64 Dantzig on workloads 1, 2
+and 4.
 """
 from __future__ import annotations
 
@@ -67,60 +69,83 @@ def class_members(plan) -> list:
 
 
 def _select(batch: LPBatch, ids) -> LPBatch:
-    """The LPs `ids` of a batch, sharing its arrays through offsets."""
+    """The LPs `ids` of a batch (repeats allowed), sharing its arrays through
+    offsets."""
     oA, ob, oc = batch.offsets()
     fam = batch.family[ids] if batch.family is not None else None
     return LPBatch(batch.m[ids], batch.n[ids], batch.A, batch.b, batch.c, off_A=oA[ids],
                    off_b=ob[ids], off_c=oc[ids], family=fam)
 
 
-def tune(batch: LPBatch, precision: str = "fp32", pricing: str = "dantzig",
-         threads=(96, 128, 160, 192, 224, 256, 320, 384, 448, 512), steps: int = 5,
-         base: dict | None = None, log=print) -> dict:
-    """Per-class table for `batch` (entries "<precision>_c<key>" and
-    "<precision>_c<key>_ctas"), starting from `base` (default: empty)."""
+def _sm_count() -> int:
+    import torch
+    return torch.cuda.get_device_properties(0).multi_processor_count
+
+
+def tune(batches: dict, precision: str = "fp32", pricing: str = "dantzig",
+         threads=(32, 64, 96, 128, 160, 192, 224, 256, 320, 384, 448, 512), steps: int = 5,
+         waves: int = 4, base: dict | None = None, log=print) -> dict:
+    """Per-class table (entries "<precision>_c<key>" and
+    "<precision>_c<key>_ctas") for the workloads `batches` (name -> LPBatch),
+    starting from `base` (default: empty)."""
     from .solver import DeviceBatch, Plan
     table = dict(base or {})
     measured = {}
     N.check(N.lib().blpg_set_tuning(json.dumps(table).encode()), "blpg_set_tuning")
-    plan = Plan(batch, precision, pricing=pricing)
-    classes = class_members(plan)
-    plan.close()
-    for key, ids, info in classes:
-        sub = _select(batch, ids)
+    members = {}
+    for name, batch in batches.items():
+        plan = Plan(batch, precision, pricing=pricing)
+        for key, ids, _ in class_members(plan):
+            members.setdefault(key, []).append((name, batch, ids))
+        plan.close()
+    sms = _sm_count()
+    for key in sorted(members):
         cps_max = key if key < 100 else 1
-        seen, results, ref = set(), [], None
+        subs = []
+        for name, batch, ids in members[key]:
+            reps = max(1, -(-waves * sms * cps_max // len(ids)))
+            sub = _select(batch, np.tile(ids, reps))
+            subs.append((name, len(ids), sub, DeviceBatch(sub, precision, pricing=pricing)))
+        rows, seen, ref = [], set(), {}
         for cps in sorted({1, 2, 3, 4, cps_max} & set(range(1, cps_max + 1))):
             for nt in threads:
                 trial = dict(table)
                 trial[f"{precision}_c{key}"] = nt
                 trial[f"{precision}_c{key}_ctas"] = cps
-                N.lib().blpg_set_tuning(json.dumps(trial).encode())
-                db = DeviceBatch(sub, precision, pricing=pricing)
-                cls = db.plan.classes()[0]
-                shape = (cls["threads"], cls["ctas_per_sm"])
-                if shape in seen:
+                N.check(N.lib().blpg_set_tuning(json.dumps(trial).encode()), "blpg_set_tuning")
+                shapes = []
+                for name, _, sub, db in subs:
                     db.plan.close()
+                    db.plan = Plan(sub, precision, pricing=pricing)
+                    cls = [c for c in db.plan.classes() if c["key"] == key][0]
+                    shapes.append((cls["threads"], cls["ctas_per_sm"]))
+                if tuple(shapes) in seen:  # the plans capped this candidate to one already timed
                     continue
-                seen.add(shape)
-                ms = _time(db, steps)
-                r = db.result()
-                if ref is None:
-                    ref = r
-                same = bool(np.array_equal(r.status, ref.status))
-                results.append(dict(threads=nt, ctas=cps, actual=list(shape), ms=ms,
-                                    statuses_equal=same))
+                seen.add(tuple(shapes))
+                times, same = [], True
+                for name, _, sub, db in subs:
+                    times.append(_time(db, steps))
+                    st = db.result().status
+                    ref.setdefault(name, st)
+                    same &= bool(np.array_equal(st, ref[name]))
+                rows.append(dict(threads=nt, ctas=cps, actual=[list(x) for x in shapes],
+                                 ms=dict(zip([s[0] for s in subs], times)), statuses_equal=same))
                 if log:
-                    log(f"{precision} class {key} ({len(ids)} LPs): threads {shape[0]:4d} "
-                        f"CTAs/SM {shape[1]:2d}: {ms:8.3f} ms")
-                db.plan.close()
-        ok = [r for r in results if r["statuses_equal"]]
+                    log(f"{precision} class {key}: threads {nt:4d} CTAs/SM {cps:2d} -> "
+                        + ", ".join(f"{s[0]} {t:8.3f} ms" for s, t in zip(subs, times)))
+        for *_, db in subs:
+            db.plan.close()
+        ok = [r for r in rows if r["statuses_equal"]]
         if ok:
-            best = min(ok, key=lambda r: r["ms"])
-            # the shape the plan actually took (residency follows occupancy)
-            table[f"{precision}_c{key}"] = best["actual"][0]
-            table[f"{precision}_c{key}_ctas"] = best["actual"][1]
-        measured[f"{precision}_c{key}"] = dict(lps=int(len(ids)), results=results)
+            best_ms = {name: min(r["ms"][name] for r in ok) for name, *_ in subs}
+            for r in ok:
+                r["score"] = sum(r["ms"][name] / best_ms[name] for name in best_ms)
+            best = min(ok, key=lambda r: r["score"])
+            # the entries as requested: a plan maps them to the same shapes
+            table[f"{precision}_c{key}"] = best["threads"]
+            table[f"{precision}_c{key}_ctas"] = best["ctas"]
+        measured[f"{precision}_c{key}"] = dict(
+            lps={name: n for name, n, *_ in subs}, waves=waves, results=rows)
     N.lib().blpg_set_tuning(None)
     table.setdefault("measured", {}).update(measured)
     return table
@@ -150,22 +175,24 @@ def reset() -> None:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--count", type=int, default=4096)
     ap.add_argument("--out", default="tuning.json")
+    ap.add_argument("--waves", type=int, default=4)
     args = ap.parse_args()
-    table = {}
-    runs = [(3, "fp32", "steepest"), (4, "fp32", "steepest"), (4, "fp64", "dantzig")]
-    for kind, prec, pricing in runs:
-        batch = generate(kind, args.count, share_family_A=True)
-        tuned = tune(batch, prec, pricing=pricing, base={})
-        for k, v in tuned.items():
-            if k == "measured":
-                table.setdefault("measured", {})[f"kind{kind}_{prec}_{pricing}"] = v
-            elif k not in table:  # the first workload that tunes a class keeps it
-                table[k] = v
+    sizes = {0: 1024, 1: 10_000, 2: 2048, 3: 10_000, 4: 20_000}
+    work = {k: generate(k, n, share_family_A=k in (3, 4)) for k, n in sizes.items()}
+    runs = [("fp32", "steepest", (0, 1, 2, 3, 4)), ("fp64", "dantzig", (1, 2, 4))]
+    table = {"measured": {}}
+    for prec, pricing, kinds in runs:
+        tuned = tune({f"kind{k}": work[k] for k in kinds}, prec, pricing=pricing,
+                     waves=args.waves, base={})
+        table["measured"].update({f"{k}_{pricing}": v for k, v in tuned.pop("measured").items()})
+        table.update(tuned)
+    table["how"] = ("python -m simplexprojects_gb300.autotune: per class key, the class's LPs of "
+                    "each workload repeated to %d waves of the GPU; the lowest sum of time over "
+                    "each workload's best time" % args.waves)
     Path(args.out).parent.mkdir(parents=True, exist_ok=True)
     Path(args.out).write_text(json.dumps(table, indent=1))
-    print(json.dumps({k: v for k, v in table.items() if k != "measured"}))
+    print(json.dumps({k: v for k, v in table.items() if k not in ("measured", "how")}))
 
 
 if __name__ == "__main__":
