@@ -514,7 +514,9 @@ def main():
         "mean_pivots": float(pivots.mean()),
         "status_counts": np.bincount(res.status, minlength=7).tolist(),
         "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "LPs/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                "step_ms_all": [round(t * 1e3, 3) for t in e2e_times],
+                "call": "blpg_solve_batch", "chunks": int(N.lib().blpg_solve_batch_chunks())},
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),

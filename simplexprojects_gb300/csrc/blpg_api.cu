@@ -980,16 +980,23 @@ static bool plan_layout_matches(const Workspace& w, const blpg_batch* bt, const 
 }  // namespace blpg
 
 // ---------------------------------------------------------------------------
-// Chunked host-buffer solve: a packed batch (no offset arrays) whose uploads
-// are large, or that does not fit the device's free memory, is split into
+// Chunked host-buffer solve.  A batch whose uploads are large is split into
 // contiguous chunks of LPs with about equal A volume, each with its own plan
-// and stream.  Chunk k's uploads run on its stream while chunk k - 1 solves
-// (the reference overlaps its copies and kernels over N streams the same
-// way, simplex.cu:914-955), and its results come back as soon as it is done.
-// When the whole batch does not fit, chunks take turns in two device regions
-// (a chunk waits for the one two before it to finish with its region), which
-// replaces the reference's host-side split by device memory
-// (GPU_Tester.cu:194-238, 284-354).
+// and stream; the uploads run one chunk after another on one stream and each
+// chunk starts solving as soon as its own data has landed, so that the
+// uploads overlap the solves of the chunks before them (the reference
+// overlaps its copies and kernels over N streams, simplex.cu:914-955).
+//
+// Two layouts on the device:
+//  * mirror: one device copy of the caller's arrays, offsets as given; chunk
+//    k uploads the part of A, b and c below the highest element its LPs read
+//    that earlier chunks did not already upload (any offsets work: an LP
+//    reading far ahead only makes its chunk wait longer);
+//  * ring: a packed batch whose inputs and outputs exceed the device budget
+//    takes turns in two regions sized for the largest chunk, each chunk
+//    relocated to its region's start (a chunk waits until the one two before
+//    it has downloaded its results), in place of the reference's host-side
+//    split by device memory (GPU_Tester.cu:194-238, 284-354).
 // ---------------------------------------------------------------------------
 namespace blpg {
 
@@ -1003,13 +1010,14 @@ struct ChunkCache {
   void* buf = nullptr;
   size_t cap = 0;
   std::vector<blpg_plan*> plans;
-  std::vector<cudaEvent_t> done;    // per region: its last chunk's downloads are enqueued
+  std::vector<cudaEvent_t> done;    // per chunk: its downloads are enqueued
   std::vector<cudaEvent_t> landed;  // per chunk: its uploads are enqueued
   cudaStream_t up = nullptr;        // every chunk's uploads, in chunk order
-  std::vector<int32_t> bounds;    // LP index of each chunk's start, then count
+  std::vector<int32_t> bounds;      // LP index of each chunk's start, then count
   std::vector<int32_t> key_shapes, key_negs;
+  std::vector<int64_t> key_offs;
   blpg_options key_opt{};
-  int key_tuning = -1, ring = 0;
+  int key_tuning = -1, ring = -1;  // ring 0: mirror layout
   void clear() {
     for (auto* pl : plans) blpg_plan_destroy(pl);
     plans.clear();
@@ -1022,7 +1030,7 @@ struct ChunkCache {
 static ChunkCache g_chunks;
 static std::atomic<int> g_last_chunks{0};  // chunks of the last blpg_solve_batch (1 = one plan)
 
-// Chunk bounds with about equal A volume, at least `per` LPs each.
+// Chunk bounds with about equal A volume.
 static std::vector<int32_t> chunk_bounds(const blpg_batch* bt, int chunks) {
   const int N = bt->count;
   int64_t total = 0;
@@ -1041,21 +1049,42 @@ static std::vector<int32_t> chunk_bounds(const blpg_batch* bt, int chunks) {
 
 // Returns BLPG_OK after solving, or 1 when the batch is not for this path.
 static int32_t solve_chunked(const blpg_batch* bt, const blpg_options& opt, blpg_result* out,
-                             const std::vector<int32_t>& shapes) {
-  if (bt->off_A || bt->off_b || bt->off_c) return 1;
+                             const std::vector<int32_t>& shapes, const std::vector<int64_t>& offs) {
   const int N = bt->count;
-  int64_t eA = 0, eb = 0, ec = 0;
-  for (int k = 0; k < N; ++k) {
-    eA += (int64_t)bt->m[k] * bt->n[k];
-    eb += bt->m[k];
-    ec += bt->n[k];
+  const bool packed = !bt->off_A && !bt->off_b && !bt->off_c;
+  // absolute offsets (the packed prefix where an offset array is absent),
+  // the packed prefixes of basis, hint and weights, and the highest element
+  // of A, b and c that LPs 0..k-1 read
+  std::vector<int64_t> oA(N), ob(N), oc(N), pB(N + 1, 0), pW(N + 1, 0);
+  std::vector<int64_t> hA(N + 1, 0), hb(N + 1, 0), hc(N + 1, 0);
+  {
+    int64_t pa = 0, pbb = 0, pc = 0;
+    for (int k = 0; k < N; ++k) {
+      const int m = bt->m[k], n = bt->n[k];
+      if (m < 0 || n < 0) return 1;
+      oA[k] = bt->off_A ? bt->off_A[k] : pa;
+      ob[k] = bt->off_b ? bt->off_b[k] : pbb;
+      oc[k] = bt->off_c ? bt->off_c[k] : pc;
+      if (oA[k] < 0 || ob[k] < 0 || oc[k] < 0) return 1;  // the one-plan path reports it
+      pa += (int64_t)m * n;
+      pbb += m;
+      pc += n;
+      pB[k + 1] = pB[k] + m;
+      pW[k + 1] = pW[k] + m + n;
+      hA[k + 1] = std::max(hA[k], oA[k] + (int64_t)m * n);
+      hb[k + 1] = std::max(hb[k], ob[k] + m);
+      hc[k + 1] = std::max(hc[k], oc[k] + n);
+    }
   }
-  const size_t h2d = sizeof(double) * (size_t)(eA + eb + ec);
+  const size_t h2d = sizeof(double) * (size_t)(hA[N] + hb[N] + hc[N]);
   size_t free_b = 0, total_b = 0;
   int ndev = 0;  // no usable device: the one-plan path reports it
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || opt.device < 0 || opt.device >= ndev) return 1;
   CK(cudaSetDevice(opt.device));
+  std::lock_guard<std::mutex> lk(g_chunks.mu);
+  ChunkCache& cc = g_chunks;
   CK(cudaMemGetInfo(&free_b, &total_b));
+  if (cc.device == opt.device) free_b += cc.cap;  // this path's own buffer is reused
   // inputs and outputs may take half the free memory (the plans' own state
   // needs the rest); the tuning table's "device_budget_mb" lowers that and
   // "overlap_mb" sets the upload volume from which copies are pipelined
@@ -1064,49 +1093,50 @@ static int32_t solve_chunked(const blpg_batch* bt, const blpg_options& opt, blpg
   if (budget_mb > 0) budget = std::min(budget, (size_t)budget_mb << 20);
   const size_t io = h2d * 5 / 4;
   const bool big = h2d >= ((size_t)tuning_value(-1, 1, (int)(kOverlapBytes >> 20)) << 20);
-  const bool tight = io > budget;
+  const bool tight = packed && io > budget;  // only a packed batch can be relocated
   if (!big && !tight) return 1;
   int chunks = std::max(2, std::min(kMaxChunks, tuning_value(-1, 3, kOverlapChunks)));
-  int ring = chunks;
+  int ring = 0;
   if (tight) {  // two regions of at most half the budget each
     ring = 2;
-    chunks = (int)std::min<size_t>(kMaxChunks, std::max<size_t>(kOverlapChunks,
+    chunks = (int)std::min<size_t>(kMaxChunks, std::max<size_t>(chunks,
                                                                 io / std::max<size_t>(1, budget / 2) + 1));
   }
   if (N < 2 * chunks) return 1;
   const bool hint = opt.basis_hint != nullptr, wt = opt.price_weight != nullptr;
   std::vector<int32_t> negs((size_t)N);
-  {
-    int64_t pb = 0;
-    for (int k = 0; k < N; ++k) {
-      int neg = 0;
-      for (int i = 0; i < bt->m[k]; ++i) neg += bt->b[pb + i] < 0.0 ? 1 : 0;
-      negs[k] = neg;
-      pb += bt->m[k];
-    }
+  for (int k = 0; k < N; ++k) {
+    int neg = 0;
+    for (int i = 0; i < bt->m[k]; ++i) neg += bt->b[ob[k] + i] < 0.0 ? 1 : 0;
+    negs[k] = neg;
   }
-  std::lock_guard<std::mutex> lk(g_chunks.mu);
-  ChunkCache& cc = g_chunks;
-  const bool reuse = !cc.plans.empty() && cc.key_shapes == shapes && cc.key_negs == negs &&
-                     same_plan_options(cc.key_opt, opt) && cc.key_tuning == tuning_generation() &&
-                     cc.ring == ring && (int)cc.plans.size() == chunks;
-  // per-chunk prefix offsets (packed layout)
+  const bool reuse = !cc.plans.empty() && cc.key_shapes == shapes && cc.key_offs == offs &&
+                     cc.key_negs == negs && same_plan_options(cc.key_opt, opt) &&
+                     cc.key_tuning == tuning_generation() && cc.ring == ring &&
+                     cc.device == opt.device;
   std::vector<int32_t> bounds = reuse ? cc.bounds : chunk_bounds(bt, chunks);
   chunks = (int)bounds.size() - 1;
-  std::vector<int64_t> pA(N + 1, 0), pB(N + 1, 0), pC(N + 1, 0), pW(N + 1, 0);
-  for (int k = 0; k < N; ++k) {
-    pA[k + 1] = pA[k] + (int64_t)bt->m[k] * bt->n[k];
-    pB[k + 1] = pB[k] + bt->m[k];
-    pC[k + 1] = pC[k] + bt->n[k];
-    pW[k + 1] = pW[k] + bt->m[k] + bt->n[k];
-  }
   if (!reuse) {
     cc.clear();
-    cc.ring = std::min(ring, chunks);
+    if (cc.device != opt.device && cc.buf) {  // the buffer is on another device
+      cudaFree(cc.buf);
+      cc.buf = nullptr;
+      cc.cap = 0;
+    }
+    cc.ring = ring;
     for (int ch = 0; ch < chunks; ++ch) {
       const int lo = bounds[ch], hi = bounds[ch + 1];
       blpg_batch sub{hi - lo, bt->m + lo, bt->n + lo, nullptr, nullptr, nullptr,
-                     bt->A + pA[lo], bt->b + pB[lo], bt->c + pC[lo]};
+                     bt->A, bt->b, bt->c};
+      if (ring) {  // packed, from the chunk's first element
+        sub.A = bt->A + oA[lo];
+        sub.b = bt->b + ob[lo];
+        sub.c = bt->c + oc[lo];
+      } else {  // the caller's offsets into the mirror
+        sub.off_A = oA.data() + lo;
+        sub.off_b = ob.data() + lo;
+        sub.off_c = oc.data() + lo;
+      }
       blpg_plan* pl = nullptr;
       int32_t rc = blpg_plan_create(&sub, &opt, &pl);
       if (rc) {
@@ -1115,53 +1145,84 @@ static int32_t solve_chunked(const blpg_batch* bt, const blpg_options& opt, blpg
       }
       cc.plans.push_back(pl);
     }
-    for (int r = 0; r < cc.ring; ++r) {
-      cudaEvent_t e;
-      CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-      cc.done.push_back(e);
-    }
     for (int ch = 0; ch < chunks; ++ch) {
-      cudaEvent_t e;
-      CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-      cc.landed.push_back(e);
+      cudaEvent_t e1, e2;
+      CK(cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
+      cc.done.push_back(e1);
+      CK(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
+      cc.landed.push_back(e2);
     }
     if (cc.up) cudaStreamDestroy(cc.up);  // on the plans' device
     cc.up = nullptr;
     CK(cudaStreamCreateWithFlags(&cc.up, cudaStreamNonBlocking));
     cc.bounds = bounds;
     cc.key_shapes = shapes;
+    cc.key_offs = offs;
     cc.key_negs = negs;
     cc.key_opt = opt;
     cc.key_tuning = tuning_generation();
+    cc.device = opt.device;
   }
-  // one region per ring slot, sized for the largest chunk
+  // device regions: A | b | c | status | objective | x | pivots | info |
+  // basis | hint | weights, 256-byte aligned; the mirror has one region for
+  // the whole batch, the ring two sized for the largest chunk
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-  size_t sA = 0, sb = 0, sc = 0, sn = 0, sw = 0;
-  for (int ch = 0; ch < chunks; ++ch) {
-    const int lo = bounds[ch], hi = bounds[ch + 1];
-    sA = std::max(sA, al(sizeof(double) * (size_t)(pA[hi] - pA[lo])));
-    sb = std::max(sb, al(sizeof(double) * (size_t)(pB[hi] - pB[lo])));
-    sc = std::max(sc, al(sizeof(double) * (size_t)(pC[hi] - pC[lo])));
-    sn = std::max(sn, al(sizeof(double) * (size_t)(hi - lo)));
-    sw = std::max(sw, al(sizeof(float) * (size_t)(pW[hi] - pW[lo])));
+  size_t sA = 0, sb = 0, sc = 0, sn = 0, sbs = 0, sw = 0;
+  const int regions = ring ? ring : 1;
+  if (ring) {
+    for (int ch = 0; ch < chunks; ++ch) {
+      const int lo = bounds[ch], hi = bounds[ch + 1];
+      sA = std::max(sA, al(sizeof(double) * (size_t)(hA[hi] - oA[lo])));
+      sb = std::max(sb, al(sizeof(double) * (size_t)(hb[hi] - ob[lo])));
+      sc = std::max(sc, al(sizeof(double) * (size_t)(hc[hi] - oc[lo])));
+      sn = std::max(sn, al(sizeof(double) * (size_t)(hi - lo)));
+      sbs = std::max(sbs, al(sizeof(int32_t) * (size_t)(pB[hi] - pB[lo])));
+      sw = std::max(sw, al(sizeof(float) * (size_t)(pW[hi] - pW[lo])));
+    }
+  } else {
+    sA = al(sizeof(double) * (size_t)hA[N]);
+    sb = al(sizeof(double) * (size_t)hb[N]);
+    sc = al(sizeof(double) * (size_t)hc[N]);
+    sn = al(sizeof(double) * (size_t)N);
+    sbs = al(sizeof(int32_t) * (size_t)pB[N]);
+    sw = al(sizeof(float) * (size_t)pW[N]);
   }
-  // A | b | c | status | objective | x | pivots | info | basis | hint | weights
-  const size_t region = sA + sb + sc + 4 * sn + sc + 2 * sb + sw;
-  const size_t need = region * (size_t)cc.ring;
-  if (cc.cap < need || cc.device != opt.device) {
+  const size_t region = sA + sb + sc + 4 * sn + sc + 2 * sbs + sw;
+  const size_t need = region * (size_t)regions;
+  if (cc.cap < need) {
     for (auto* pl : cc.plans) cudaStreamSynchronize(pl->stream);
     if (cc.buf) cudaFree(cc.buf);
     cc.buf = nullptr;
     cc.cap = 0;
     CK(cudaMalloc(&cc.buf, need));
     cc.cap = need;
-    cc.device = opt.device;
   }
-  // Downloads into pageable host memory block the calling thread until the
-  // chunk is solved, so chunk j's downloads are enqueued only after the
-  // uploads and solve of chunk j + ring - 1 (the last chunk that can still
-  // start before chunk j's region is needed again).
+  struct Region {
+    double *A, *b, *c, *obj, *x;
+    int32_t *status, *pivots, *info, *basis, *hint;
+    float* w;
+  };
+  auto region_at = [&](int r) {
+    char* o = (char*)cc.buf + (size_t)r * region;
+    Region g;
+    g.A = (double*)o, o += sA;
+    g.b = (double*)o, o += sb;
+    g.c = (double*)o, o += sc;
+    g.status = (int32_t*)o, o += sn;
+    g.obj = (double*)o, o += sn;
+    g.pivots = (int32_t*)o, o += sn;
+    g.info = (int32_t*)o, o += sn;
+    g.x = (double*)o, o += sc;
+    g.basis = (int32_t*)o, o += sbs;
+    g.hint = (int32_t*)o, o += sbs;
+    g.w = (float*)o;
+    return g;
+  };
+  // Per chunk: the device pointers its plan reads and writes, and the host
+  // ranges its uploads and downloads cover (element offsets into the
+  // caller's arrays, and into the region).
   std::vector<blpg_result> dres((size_t)chunks);
+  int64_t upA = 0, upb = 0, upc = 0;  // mirror: elements uploaded so far
   auto download = [&](int ch) -> int32_t {
     blpg_plan* pl = cc.plans[ch];
     cudaStream_t s = pl->stream;
@@ -1170,9 +1231,6 @@ static int32_t solve_chunked(const blpg_batch* bt, const blpg_options& opt, blpg
     CK(cudaMemcpyAsync(out->status + lo, d.status, sizeof(int32_t) * cn, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(out->objective + lo, d.objective, sizeof(double) * cn,
                        cudaMemcpyDeviceToHost, s));
-    if (out->x)
-      CK(cudaMemcpyAsync(out->x + pC[lo], d.x, sizeof(double) * (size_t)(pC[hi] - pC[lo]),
-                         cudaMemcpyDeviceToHost, s));
     if (out->pivots)
       CK(cudaMemcpyAsync(out->pivots + lo, d.pivots, sizeof(int32_t) * cn, cudaMemcpyDeviceToHost,
                          s));
@@ -1181,62 +1239,120 @@ static int32_t solve_chunked(const blpg_batch* bt, const blpg_options& opt, blpg
     if (out->basis)
       CK(cudaMemcpyAsync(out->basis + pB[lo], d.basis,
                          sizeof(int32_t) * (size_t)(pB[hi] - pB[lo]), cudaMemcpyDeviceToHost, s));
-    CK(cudaEventRecord(cc.done[ch % cc.ring], s));
+    if (out->x) {  // x of LP k sits where its c does
+      int64_t lo_c = oc[lo], hi_c = oc[lo];
+      for (int k = lo; k < hi; ++k) {
+        lo_c = std::min(lo_c, oc[k]);
+        hi_c = std::max(hi_c, oc[k] + bt->n[k]);
+      }
+      const double* src = ring ? d.x + (lo_c - oc[lo]) : d.x + lo_c;
+      CK(cudaMemcpyAsync(out->x + lo_c, src, sizeof(double) * (size_t)(hi_c - lo_c),
+                         cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaEventRecord(cc.done[ch], s));
     return BLPG_OK;
   };
-  int32_t rc = BLPG_OK;
-  for (int ch = 0; ch < chunks; ++ch) {
-    blpg_plan* pl = cc.plans[ch];
-    cudaStream_t s = pl->stream, u = cc.up;
-    const int r = ch % cc.ring;
-    // uploads go one chunk after another on one stream, so that each chunk
-    // lands at the full copy bandwidth (concurrent copies would share it and
-    // land together); a region is reused once its last chunk's downloads ran
-    if (ch >= cc.ring) CK(cudaStreamWaitEvent(u, cc.done[r], 0));
-    char* o = (char*)cc.buf + (size_t)r * region;
-    double* dA = (double*)o;
-    o += sA;
-    double* db = (double*)o;
-    o += sb;
-    double* dc = (double*)o;
-    o += sc;
+  // Downloads into pageable host memory block the calling thread until the
+  // chunk is solved, so chunk j's downloads are enqueued only after the
+  // uploads and solve of chunk j + lag have been (lag = ring - 1: the last
+  // chunk that can start before chunk j's region is needed again; the
+  // mirror enqueues every chunk first).
+  std::vector<double*> dA((size_t)chunks), db((size_t)chunks), dc((size_t)chunks);
+  std::vector<int32_t*> dhint((size_t)chunks, nullptr);
+  std::vector<float*> dw((size_t)chunks, nullptr);
+  auto upload = [&](int ch) -> int32_t {
+    cudaStream_t u = cc.up;
     const int lo = bounds[ch], hi = bounds[ch + 1];
+    const Region g = region_at(ring ? ch % ring : 0);
+    if (ring && ch >= ring) CK(cudaStreamWaitEvent(u, cc.done[ch - ring], 0));
     blpg_result& d = dres[ch];
     d = blpg_result{};
-    d.status = (int32_t*)o;
-    o += sn;
-    d.objective = (double*)o;
-    o += sn;
-    d.x = out->x ? (double*)o : nullptr;
-    o += sc;
-    d.pivots = out->pivots ? (int32_t*)o : nullptr;
-    o += sn;
-    d.info = out->info ? (int32_t*)o : nullptr;
-    o += sn;
-    d.basis = out->basis ? (int32_t*)o : nullptr;
-    int32_t* dhint = hint ? (int32_t*)(o + sb) : nullptr;
-    o += 2 * sb;
-    float* dw = wt ? (float*)o : nullptr;
-    CK(cudaMemcpyAsync(dA, bt->A + pA[lo], sizeof(double) * (size_t)(pA[hi] - pA[lo]),
-                       cudaMemcpyHostToDevice, u));
-    CK(cudaMemcpyAsync(db, bt->b + pB[lo], sizeof(double) * (size_t)(pB[hi] - pB[lo]),
-                       cudaMemcpyHostToDevice, u));
-    CK(cudaMemcpyAsync(dc, bt->c + pC[lo], sizeof(double) * (size_t)(pC[hi] - pC[lo]),
-                       cudaMemcpyHostToDevice, u));
+    dA[ch] = g.A;
+    db[ch] = g.b;
+    dc[ch] = g.c;
+    if (ring) {  // relocated to the region's start
+      CK(cudaMemcpyAsync(g.A, bt->A + oA[lo], sizeof(double) * (size_t)(hA[hi] - oA[lo]),
+                         cudaMemcpyHostToDevice, u));
+      CK(cudaMemcpyAsync(g.b, bt->b + ob[lo], sizeof(double) * (size_t)(hb[hi] - ob[lo]),
+                         cudaMemcpyHostToDevice, u));
+      CK(cudaMemcpyAsync(g.c, bt->c + oc[lo], sizeof(double) * (size_t)(hc[hi] - oc[lo]),
+                         cudaMemcpyHostToDevice, u));
+      d.status = g.status;
+      d.objective = g.obj;
+      d.pivots = out->pivots ? g.pivots : nullptr;
+      d.info = out->info ? g.info : nullptr;
+      d.x = out->x ? g.x : nullptr;
+      d.basis = out->basis ? g.basis : nullptr;
+      dhint[ch] = hint ? g.hint : nullptr;
+      dw[ch] = wt ? g.w : nullptr;
+    } else {  // the mirror: whatever LPs lo..hi-1 read that is not there yet
+      if (hA[hi] > upA)
+        CK(cudaMemcpyAsync(g.A + upA, bt->A + upA, sizeof(double) * (size_t)(hA[hi] - upA),
+                           cudaMemcpyHostToDevice, u));
+      if (hb[hi] > upb)
+        CK(cudaMemcpyAsync(g.b + upb, bt->b + upb, sizeof(double) * (size_t)(hb[hi] - upb),
+                           cudaMemcpyHostToDevice, u));
+      if (hc[hi] > upc)
+        CK(cudaMemcpyAsync(g.c + upc, bt->c + upc, sizeof(double) * (size_t)(hc[hi] - upc),
+                           cudaMemcpyHostToDevice, u));
+      upA = std::max(upA, hA[hi]);
+      upb = std::max(upb, hb[hi]);
+      upc = std::max(upc, hc[hi]);
+      d.status = g.status + lo;
+      d.objective = g.obj + lo;
+      d.pivots = out->pivots ? g.pivots + lo : nullptr;
+      d.info = out->info ? g.info + lo : nullptr;
+      d.x = out->x ? g.x : nullptr;  // written at the LPs' own c offsets
+      d.basis = out->basis ? g.basis + pB[lo] : nullptr;
+      dhint[ch] = hint ? g.hint + pB[lo] : nullptr;
+      dw[ch] = wt ? g.w + pW[lo] : nullptr;
+    }
     if (hint)
-      CK(cudaMemcpyAsync(dhint, opt.basis_hint + pB[lo], sizeof(int32_t) * (size_t)(pB[hi] - pB[lo]),
-                         cudaMemcpyHostToDevice, u));
+      CK(cudaMemcpyAsync(dhint[ch], opt.basis_hint + pB[lo],
+                         sizeof(int32_t) * (size_t)(pB[hi] - pB[lo]), cudaMemcpyHostToDevice, u));
     if (wt)
-      CK(cudaMemcpyAsync(dw, opt.price_weight + pW[lo], sizeof(float) * (size_t)(pW[hi] - pW[lo]),
-                         cudaMemcpyHostToDevice, u));
+      CK(cudaMemcpyAsync(dw[ch], opt.price_weight + pW[lo],
+                         sizeof(float) * (size_t)(pW[hi] - pW[lo]), cudaMemcpyHostToDevice, u));
     CK(cudaEventRecord(cc.landed[ch], u));
+    return BLPG_OK;
+  };
+  auto launch = [&](int ch) -> int32_t {
+    cudaStream_t s = cc.plans[ch]->stream;
     CK(cudaStreamWaitEvent(s, cc.landed[ch], 0));
-    if ((rc = blpg_plan_execute_weighted(pl, dA, db, dc, dhint, dw, &d, s))) return rc;
-    if (ch - (cc.ring - 1) >= 0 && (rc = download(ch - (cc.ring - 1)))) return rc;
+    return blpg_plan_execute_weighted(cc.plans[ch], dA[ch], db[ch], dc[ch], dhint[ch], dw[ch],
+                                      &dres[ch], s);
+  };
+  // Enqueue order.  Uploads from pinned memory return at once: every upload
+  // of the mirror is enqueued before any solve, so that no copy is queued in
+  // a hardware channel behind a solve that waits for a later copy (with a
+  // plan per chunk and a graph branch per size class, streams share the
+  // device's few channels).  Uploads from pageable memory return only once
+  // staged, so they alternate with the solves, each chunk's solve enqueued
+  // as soon as its uploads are.  The ring alternates too: a region's next
+  // upload waits for its previous chunk's downloads.
+  cudaPointerAttributes pa{};
+  const bool pinned = cudaPointerGetAttributes(&pa, bt->A) == cudaSuccess &&
+                      pa.type == cudaMemoryTypeHost;
+  cudaGetLastError();  // a pageable pointer may leave an error on older runtimes
+  const int lag = ring ? ring - 1 : chunks - 1;
+  int32_t rc = BLPG_OK;
+  if (!ring && pinned) {
+    for (int ch = 0; ch < chunks; ++ch)
+      if ((rc = upload(ch))) return rc;
+    for (int ch = 0; ch < chunks; ++ch)
+      if ((rc = launch(ch))) return rc;
+    for (int ch = 0; ch < chunks; ++ch)
+      if ((rc = download(ch))) return rc;
+  } else {
+    for (int ch = 0; ch < chunks; ++ch) {
+      if ((rc = upload(ch)) || (rc = launch(ch))) return rc;
+      if (ch - lag >= 0 && (rc = download(ch - lag))) return rc;
+    }
+    for (int ch = std::max(0, chunks - lag); ch < chunks; ++ch)
+      if ((rc = download(ch))) return rc;
   }
-  for (int ch = std::max(0, chunks - cc.ring + 1); ch < chunks; ++ch)
-    if ((rc = download(ch))) return rc;
   for (auto* pl : cc.plans) CK(cudaStreamSynchronize(pl->stream));
+  CK(cudaStreamSynchronize(cc.up));
   CK(cudaGetLastError());
   g_last_chunks = chunks;
   return BLPG_OK;
@@ -1291,7 +1407,7 @@ extern "C" int32_t blpg_solve_batch(const blpg_batch* bt, const blpg_options* op
   if (wt && opt.pricing != BLPG_PRICE_STEEPEST)
     return fail(BLPG_EINVAL, "blpg_solve_batch: pricing weights need steepest-edge pricing");
   {
-    const int32_t rc0 = solve_chunked(bt, opt, out, shapes);
+    const int32_t rc0 = solve_chunked(bt, opt, out, shapes, offs);
     if (rc0 != 1) return rc0;  // solved in chunks (or failed there)
   }
   g_last_chunks = 1;

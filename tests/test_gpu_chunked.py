@@ -73,3 +73,33 @@ def test_chunked_warm_start_inputs(built):
     assert np.array_equal(one.pivots, eight.pivots)
     assert np.array_equal(one.info, eight.info)
     assert np.array_equal(one.objective.view(np.uint64), eight.objective.view(np.uint64))
+
+
+@pytest.mark.parametrize("knobs,chunks", [({"overlap_mb": 8}, 8), ({"overlap_mb": 8, "overlap_chunks": 5}, 5),
+                                          ({"device_budget_mb": 4}, 8)])
+def test_chunked_solve_with_offsets(built, knobs, chunks):
+    """A batch given by offset arrays (LPs of a family share one A) is solved
+    in chunks on one device copy of the caller's arrays, each chunk uploading
+    what its LPs read beyond what earlier chunks uploaded.  It is never
+    relocated (its LPs may read any part of A), so a device budget does not
+    split it further."""
+    batch = sp.generate(4, 3000, seed=sp.DEFAULT_SEED, share_family_A=True)
+    assert batch.off_A is not None
+    cpu = ref.solve_batch(batch, "fp64", want_x=True, want_basis=True)
+    try:
+        _tuning(knobs)
+        g = sp.solve(batch, "fp64", want_x=True, want_basis=True)
+        used = N.lib().blpg_solve_batch_chunks()
+        f = sp.solve(batch, "fp32", pricing="steepest", want_x=True)
+    finally:
+        N.check(N.lib().blpg_set_tuning(None), "blpg_set_tuning")
+    assert used == chunks
+    assert np.array_equal(g.status, cpu.status)
+    assert np.array_equal(g.pivots, cpu.pivots)
+    assert np.array_equal(g.basis, cpu.basis)
+    assert np.array_equal(g.objective.view(np.uint64), cpu.objective.view(np.uint64))
+    assert np.array_equal(g.x.view(np.uint64), cpu.x.view(np.uint64))
+    opt = cpu.status == 5
+    assert np.array_equal(f.status, cpu.status)
+    rel = np.abs(f.objective - cpu.objective) / np.maximum(np.abs(cpu.objective), 1.0)
+    assert rel[opt].max() <= 1e-6
