@@ -188,9 +188,13 @@ enum {
                                 (unverified, at its pivot cap 4 (m + n) + 200, or
                                 "infeasible" with b >= 0); the plan's FP64 pass solved it
                                 from scratch with the FP64 Dantzig method */
-  BLPG_INFO_RETRY = 2048     /* a warm-started solve ended on a basis the FP64 check could
+  BLPG_INFO_RETRY = 2048,    /* a warm-started solve ended on a basis the FP64 check could
                                 not verify and was re-run cold from the slack basis (one that
                                 hits the pivot cap is re-run too, with BLPG_INFO_FALLBACK) */
+  BLPG_INFO_LOAD = 4096      /* the bulk (TMA) copies loading the LP's tableau did not
+                                complete within the kernel's wait limit: status UNDEF, and the
+                                CTA that held it stopped taking LPs (never expected; it keeps
+                                a stuck copy from hanging the device) */
 };
 
 /* Fill *opt with the defaults above. */

@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <memory>
 #include <atomic>
 #include <mutex>
@@ -116,8 +117,15 @@ struct blpg_plan {
   std::vector<int32_t> order;
   // device arrays
   int32_t *d_m = nullptr, *d_n = nullptr, *d_order = nullptr, *d_tickets = nullptr;
-  int64_t *d_off = nullptr;  // offA | offb | offc | offx | offbasis
-  float* d_A32 = nullptr;    // FP32 plans: A rounded to FP32, elements [minA, extA) filled
+  int64_t *d_off = nullptr;  // offA | offb | offc | offx | offbasis | offw | off32
+  // FP32 plans whose LPs share A: every distinct block of A (offset, m, n)
+  // rounded to FP32 once per execute, rows padded to the single-CTA tableau
+  // row (a32_pitch) so that the loader takes a block in one bulk copy;
+  // d_blk holds offA, off32, m, n per block
+  float* d_A32 = nullptr;
+  int64_t* d_blk = nullptr;
+  int nblk = 0;
+  int max_blk_rows = 0;
   double* d_lu = nullptr;    // LU refresh scratch of every class (FP32, FP64 steepest edge)
   size_t lu_doubles = 0;
   // FP32 plans: the FP64 pass, one persistent FP64 launch over the LPs the
@@ -147,6 +155,7 @@ static void release(blpg_plan* p) {
   cudaFree(p->d_tickets);
   cudaFree(p->d_off);
   cudaFree(p->d_A32);
+  cudaFree(p->d_blk);
   cudaFree(p->d_lu);
   cudaFree(p->d_fb);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
@@ -482,14 +491,24 @@ static int launch_fallback(blpg_plan* p, const LpArgs& args, cudaStream_t s) {
 
 // Queue reset, then every class on its own stream (fork/join through
 // events, so a captured graph has one parallel branch per class).
-// A rounded to FP32 for FP32 tableau loads: elements [lo, hi) of A, the same
-// rounding as the in-kernel loader's (f64_to_f32_rn); a grid-stride pass at
-// HBM speed.
+// A rounded to FP32 for FP32 tableau loads: every distinct block of A (blk:
+// offA, off32, m, n), the same rounding as the in-kernel loader's
+// (f64_to_f32_rn), rows padded with zeros to a32_pitch(n) elements.  A
+// warp per row (blocks along y, rows along x, grid-stride), reads and writes
+// coalesced along the row: one pass at HBM speed.
 __global__ void round_a32_kernel(const double* __restrict__ A, float* __restrict__ A32,
-                                 long long lo, long long hi) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long e = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x; e < hi; e += stride)
-    A32[e] = dev::f64_to_f32_rn(__ldg(A + e));
+                                 const long long* __restrict__ blk, int nblk) {
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  for (int bk = blockIdx.y; bk < nblk; bk += gridDim.y) {
+    const long long offA = blk[4 * bk], off32 = blk[4 * bk + 1];
+    const int m = (int)blk[4 * bk + 2], n = (int)blk[4 * bk + 3], ld = dev::a32_pitch(n);
+    for (int i = blockIdx.x * wpb + (threadIdx.x >> 5); i < m; i += gridDim.x * wpb) {
+      const double* src = A + offA + (long long)i * n;
+      float* dst = A32 + off32 + (long long)i * ld;
+      for (int j = lane; j < ld; j += 32) dst[j] = j < n ? dev::f64_to_f32_rn(__ldg(src + j)) : 0.f;
+    }
+  }
 }
 
 // The same rounding over a plain array, or CUDA's conversion instruction
@@ -508,10 +527,11 @@ static int launch_classes(blpg_plan* p, const LpArgs& args, cudaStream_t s) {
   const size_t nc = p->classes.size();
   if (nc == 0) return BLPG_OK;
   if (args.A32) {  // A rounded to FP32 before any class loads a tableau
-    const long long span = p->extA - p->minA;
-    const int grid = (int)std::min<long long>((span + 255) / 256, 8LL * std::max(1, p->sm_count));
-    round_a32_kernel<<<grid, 256, 0, s>>>(args.A, const_cast<float*>(args.A32), p->minA,
-                                               p->extA);
+    const int gx = std::max(1, std::min(dev::ceil_div(p->max_blk_rows, 8), 64));
+    const int gy = std::max(1, std::min(p->nblk, 8 * std::max(1, p->sm_count) / gx + 1));
+    round_a32_kernel<<<dim3(gx, gy), 256, 0, s>>>(args.A, const_cast<float*>(args.A32),
+                                                  reinterpret_cast<const long long*>(p->d_blk),
+                                                  p->nblk);
     CK(cudaGetLastError());
   }
   CK(cudaEventRecord(p->ev_fork, s));
@@ -720,7 +740,7 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
   CKF(cudaMalloc(&p->d_n, sizeof(int32_t) * Nn));
   CKF(cudaMalloc(&p->d_order, sizeof(int32_t) * Nn));
   CKF(cudaMalloc(&p->d_tickets, sizeof(int32_t) * (nc + 1)));  // + the FP64 pass's
-  CKF(cudaMalloc(&p->d_off, sizeof(int64_t) * 6 * Nn));
+  CKF(cudaMalloc(&p->d_off, sizeof(int64_t) * 7 * Nn));
   // FP32 tableaux load A from an FP32 copy rounded once per execute (one
   // bandwidth-bound pass) when LPs share A: every element of A's extent read
   // by two LPs or more on average.  With an A per LP the copy would be an
@@ -728,8 +748,27 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
   // conversion overlaps other CTAs' pivots).
   int64_t readA = 0;
   for (int k = 0; k < N; ++k) readA += (int64_t)p->m[k] * p->n[k];
+  std::vector<int64_t> off32;
   if (p->precision == BLPG_FP32 && p->extA > p->minA && readA >= 2 * (p->extA - p->minA)) {
-    CKF(cudaMalloc(&p->d_A32, sizeof(float) * (size_t)p->extA));
+    std::map<std::tuple<int64_t, int, int>, int64_t> blocks;  // (offA, m, n) -> off32
+    std::vector<int64_t> blk;
+    off32.resize((size_t)N);
+    int64_t acc = 0;
+    for (int k = 0; k < N; ++k) {
+      const auto key = std::make_tuple(p->offA[k], p->m[k], p->n[k]);
+      auto it = blocks.find(key);
+      if (it == blocks.end()) {
+        it = blocks.emplace(key, acc).first;
+        blk.insert(blk.end(), {p->offA[k], acc, (int64_t)p->m[k], (int64_t)p->n[k]});
+        acc += (int64_t)p->m[k] * dev::a32_pitch(p->n[k]);
+        p->max_blk_rows = std::max(p->max_blk_rows, p->m[k]);
+      }
+      off32[k] = it->second;
+    }
+    p->nblk = (int)blocks.size();
+    CKF(cudaMalloc(&p->d_A32, sizeof(float) * (size_t)std::max<int64_t>(acc, 4)));
+    CKF(cudaMalloc(&p->d_blk, sizeof(int64_t) * blk.size()));
+    CKF(cudaMemcpy(p->d_blk, blk.data(), sizeof(int64_t) * blk.size(), cudaMemcpyHostToDevice));
     p->launches += 1;
   }
   if (p->precision == BLPG_FP32 && N > 0 && build_fallback(p.get(), max_smem)) {
@@ -757,7 +796,7 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
     }
   }
   if (N > 0) {
-    std::vector<int64_t> off(6 * (size_t)N);
+    std::vector<int64_t> off(7 * (size_t)N, 0);
     std::copy(p->offA.begin(), p->offA.end(), off.begin());
     std::copy(p->offb.begin(), p->offb.end(), off.begin() + N);
     std::copy(p->offc.begin(), p->offc.end(), off.begin() + 2 * N);
@@ -773,7 +812,8 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
     CKF(cudaMemcpy(p->d_n, p->n.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice));
     CKF(cudaMemcpy(p->d_order, p->order.data(), sizeof(int32_t) * N,
                    cudaMemcpyHostToDevice));
-    CKF(cudaMemcpy(p->d_off, off.data(), sizeof(int64_t) * 6 * N, cudaMemcpyHostToDevice));
+    if (!off32.empty()) std::copy(off32.begin(), off32.end(), off.begin() + 6 * N);
+    CKF(cudaMemcpy(p->d_off, off.data(), sizeof(int64_t) * 7 * N, cudaMemcpyHostToDevice));
   }
 #undef CKF
   *out = p.release();
@@ -812,6 +852,7 @@ extern "C" int32_t blpg_plan_execute_weighted(blpg_plan* p, const double* dA, co
   a.weight = price_weight;
   a.A = dA;
   a.A32 = p->d_A32;
+  a.off32 = p->d_A32 ? p->d_off + 6 * N : nullptr;
   a.fb = p->has_fb ? p->d_fb : nullptr;
   a.b = db;
   a.c = dc;

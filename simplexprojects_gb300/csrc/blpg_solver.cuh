@@ -82,7 +82,8 @@ struct LpArgs {
   int32_t pricing;         // 0: Dantzig, 1: steepest edge (exact column norms)
   const float* weight;     // nullable: steepest-edge score weight per variable (n + m per LP)
   const int64_t* offw;     // offsets of `weight`
-  const float* A32;        // nullable: A rounded to FP32 (offsets of A), read by FP32 tableau loads
+  const float* A32;        // nullable: A rounded to FP32, rows padded to a32_pitch(n)
+  const int64_t* off32;    // offsets of A32 (with A32)
   int32_t* fb;             // nullable (FP32 plans): [0] count, [1..] LPs handed to the FP64 pass
   int32_t info_or;         // bits OR'ed into every info written (the FP64 pass: kInfoFp64)
 };
@@ -100,6 +101,7 @@ constexpr int kInfoReinvert = 256;    // the tableau was rebuilt from an FP64 fa
 constexpr int kInfoFactor = 512;      // an FP64 refresh used the LU factorisation (refresh_lu)
 constexpr int kInfoFp64 = 1024;       // re-solved on an FP64 tableau (the FP64 pass of an FP32 plan)
 constexpr int kInfoRetry = 2048;      // a warm start ended unverified or at the pivot cap: re-run cold
+constexpr int kInfoLoad = 4096;       // a tableau load's bulk copies did not complete: LP given up
 
 struct ClassArgs {
   const int32_t* order;  // LP ids of this class, heaviest first
@@ -129,6 +131,10 @@ struct VecT<float> {
 
 __host__ __device__ inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
 __host__ __device__ inline int round_up(int a, int b) { return ceil_div(a, b) * b; }
+// Row pitch of the FP32 copy of A (elements): the row length of a
+// single-CTA phase-II FP32 tableau (Geom with K = 1, na = 0, V = 4), so that
+// such an LP's whole block is one contiguous copy; every row 16-byte aligned.
+__host__ __device__ inline int a32_pitch(int n) { return round_up(n, 4) + 4; }
 
 // Per-LP column geometry.  Variables 0..n-1 structural, n..n+m-1 slacks,
 // n+m..n+m+na-1 artificials (two-phase only).  The tableau stores Wc = n + na
@@ -304,6 +310,57 @@ __device__ __forceinline__ float vget<float4, float>(const float4& v, int e) {
   return e == 0 ? v.x : (e == 1 ? v.y : (e == 2 ? v.z : v.w));
 }
 
+// Bulk (TMA) copies from global to this CTA's shared memory, completing on
+// an mbarrier in shared memory: both addresses 16-byte aligned, the size a
+// multiple of 16 (the callers check both).  No cluster multicast.
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_inval(unsigned long long* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Bounded wait for phase `parity` of an mbarrier (every thread that reads
+// the copied data waits itself): false when it did not complete.
+constexpr int kBarWaitLimit = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  for (int it = 0; it < kBarWaitLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// Orders this thread's earlier generic-proxy accesses to shared memory
+// before later bulk copies into it.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 __device__ __forceinline__ double sdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ float sdiv(float a, float b) { return __fdiv_rn(a, b); }
 // Local index of global slot s on the CTA holding slots [c0, c0 + cw), -1 on
@@ -431,7 +488,7 @@ struct SharedState {
   Key pslot;
   Key aux;
   double z;       // FP64 objective of the last refresh
-  double pad2;
+  unsigned long long bar;  // mbarrier of the tableau's bulk loads (valid only during a load)
   Key gather[8];  // the cluster's pricing candidates, fetched once per CTA
 };
 
@@ -2043,7 +2100,7 @@ struct Solver {
     }
   }
 
-  // The same block from A already rounded to FP32 (A32, same offsets as A):
+  // The same block from A already rounded to FP32 (A32, rows `pitch` apart):
   // rows 0..m-1 are plain copies (half the bytes of the FP64 rows, nothing
   // to convert); row m (-c in a single-phase LP, 0 before phase I) is
   // converted separately, so that no conversion sits in the row loop.
@@ -2051,7 +2108,7 @@ struct Solver {
                                                    const float* __restrict__ const Ac,
                                                    const double* __restrict__ const cc,
                                                    const int* __restrict__ const flags,
-                                                   const int m, const int n, const int nA,
+                                                   const int m, const int pitch, const int nA,
                                                    const int ldw, const int na) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     constexpr int kR = 2, kQ = 8;
@@ -2064,7 +2121,7 @@ struct Solver {
 #pragma unroll
           for (int q = 0; q < kQ; ++q) {
             const int j = j0 + q * 32 + lane;
-            v[r][q] = j < nA ? __ldg(Ac + (size_t)i * n + j) : 0.f;
+            v[r][q] = j < nA ? __ldg(Ac + (size_t)i * pitch + j) : 0.f;
           }
         }
 #pragma unroll
@@ -2084,29 +2141,85 @@ struct Solver {
       tb[(size_t)m * ldw + j] = na == 0 ? -f64_to_f32_rn(__ldg(cc + j)) : 0.f;
   }
 
+  // FP32 tableau of a single-CTA phase-II LP from the padded FP32 copy of A,
+  // whose rows are exactly as long as the tableau's (a32_pitch(n) = ldw):
+  // the whole block, rows 0..m-1, is one bulk (TMA) copy issued by one
+  // thread and completing on the CTA's mbarrier (the rows' padding lands in
+  // slots [n, ldw), which load() fills afterwards); the objective row -c is
+  // converted meanwhile.  False when the copy did not complete within the
+  // wait limit.
+  __device__ bool load_block_bulk32(const Geom& g, const float* A32, const double* c) {
+    const int m = g.m, n = g.n, ldw = g.ldw;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    float* tb = reinterpret_cast<float*>(tab);
+    unsigned long long* bar = &sh->bar;
+    fence_proxy_async_smem();  // the previous LP's accesses to these rows come first
+    if (tid == 0) mbar_init(bar, 1);
+    __syncthreads();
+    const unsigned bytes = (unsigned)m * (unsigned)ldw * 4u;
+    if (tid == 0) {
+      mbar_arrive_expect_tx(bar, bytes);
+      if (bytes > 0) bulk_g2s(tb, A32, bytes, bar);
+    }
+    for (int j = tid; j < n; j += nt) tb[(size_t)m * ldw + j] = -f64_to_f32_rn(__ldg(c + j));
+    bool ok = mbar_wait(bar, 0);
+    if (!ok) mbar_wait(bar, 0);  // let a copy still in flight land before giving up
+    __syncthreads();
+    if (tid == 0) mbar_inval(bar);
+    return ok;
+  }
+
   // FP64 tableau: the structural block copied straight from rows of A (and
-  // c for row m of a single-phase LP) by asynchronous 8-byte global-to-shared
-  // copies, which need no registers, then the rows to negate negated in place.
-  __device__ void load_rows_async(const Geom& g, int c0, int nA, const double* A,
+  // c for row m of a single-phase LP), no registers involved.  A row whose
+  // source starts on a 16-byte boundary goes by one bulk (TMA) copy of its
+  // whole 16-byte pairs, issued by the first warp and completing on the
+  // CTA's mbarrier; the other rows, and an odd last element, by 8-byte
+  // asynchronous copies.  Then the rows to negate are negated in place.
+  // False when the bulk copies did not complete within the wait limit.
+  __device__ bool load_rows_async(const Geom& g, int c0, int nA, const double* A,
                                   const double* c) {
     const int m = g.m, n = g.n, na = g.na, ldw = g.ldw;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    const unsigned pair_bytes = (unsigned)(nA >> 1) * 16u;
+    const int npair = (nA >> 1) << 1;  // elements the bulk copy of a row covers
+    unsigned long long* bar = &sh->bar;
+    const bool tab16 = (smem_addr(tab) & 15u) == 0 && (ldw & 1) == 0;
+    auto src_of = [&](int i) { return i < m ? A + (size_t)i * n + c0 : c + c0; };
+    auto bulk_row = [&](int i) {
+      return tab16 && pair_bytes > 0 && (i < m || na == 0) &&
+             (reinterpret_cast<uintptr_t>(src_of(i)) & 15u) == 0;
+    };
+    fence_proxy_async_smem();  // the previous LP's accesses to these rows come first
+    if (tid == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (warp == 0) {
+      int rows = 0;
+      for (int i = lane; i <= m; i += 32) rows += bulk_row(i) ? 1 : 0;
+      rows = __reduce_add_sync(0xffffffffu, rows);
+      if (lane == 0) mbar_arrive_expect_tx(bar, (unsigned)rows * pair_bytes);
+      __syncwarp();
+      for (int i = lane; i <= m; i += 32)
+        if (bulk_row(i)) bulk_g2s(tab + (size_t)i * ldw, src_of(i), pair_bytes, bar);
+    }
     for (int i = warp; i <= m; i += nw) {
       T* dst = tab + (size_t)i * ldw;
       if (i == m && na > 0) {  // phase I starts from a zero objective row
         for (int j = lane; j < nA; j += 32) dst[j] = T(0);
         continue;
       }
-      const double* src = i < m ? A + (size_t)i * n + c0 : c + c0;
-      for (int j = lane; j < nA; j += 32) {
-        const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + j);
+      const double* src = src_of(i);
+      for (int j = (bulk_row(i) ? npair : 0) + lane; j < nA; j += 32) {
+        const unsigned sa = smem_addr(dst + j);
         asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(src + j)
                      : "memory");
       }
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
     asm volatile("cp.async.wait_group 0;" ::: "memory");
+    bool ok = mbar_wait(bar, 0);
+    if (!ok) mbar_wait(bar, 0);  // let copies still in flight land before giving up
     __syncthreads();
+    if (tid == 0) mbar_inval(bar);
     // -c in the objective row of a single-phase LP; the rows with b_i < 0
     for (int i = warp; i <= m; i += nw) {
       const bool neg = i == m ? na == 0 : (na > 0 && flags[i] >= 0);
@@ -2114,14 +2227,33 @@ struct Solver {
       T* row = tab + (size_t)i * ldw;
       for (int j = lane; j < nA; j += 32) row[j] = -row[j];
     }
+    return ok;
   }
 
   // Build the slack-basis tableau of LP lp: rows with b_i < 0 are negated
   // and get an artificial variable each (the a-th such row's artificial is
   // basic there and its slack takes column slot n + a); structural j sits in
   // slot j.  Coalesced along rows of A.
+  // Out of line, on a copy of the solver (load changes no member), so that
+  // the loaders' registers do not add to the pivot loop's.  When the bulk
+  // copies of the load do not complete within the wait limit, LP lp is given
+  // up (abandon) and the CTA -- every CTA of its cluster, which decide
+  // together -- exits; the kernel's other CTAs go on.
+  static __device__ __noinline__ void load_call(Solver self, const Geom g, int c0, int lc,
+                                                const double* A, const double* b,
+                                                const double* c, const float* A32,
+                                                const LpArgs& a, int lp) {
+    if (!self.load_body(g, c0, lc, A, b, c, A32)) {
+      self.abandon(a, lp);
+      asm volatile("exit;" ::: "memory");
+    }
+  }
   __device__ void load(const Geom& g, int c0, int lc, const double* A, const double* b,
-                       const double* c, const float* A32 = nullptr) {
+                       const double* c, const float* A32, const LpArgs& a, int lp) {
+    load_call(*this, g, c0, lc, A, b, c, A32, a, lp);
+  }
+  __device__ bool load_body(const Geom& g, int c0, int lc, const double* A, const double* b,
+                            const double* c, const float* A32) {
     const int tid = threadIdx.x, nt = blockDim.x;
     const int m = g.m, n = g.n, na = g.na;
     const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
@@ -2177,12 +2309,26 @@ struct Solver {
     // Structural block (slots [0, nA) of this CTA); row m is the objective
     // row (-c in a single-phase LP, 0 before phase I)
     const int nA = max(0, min(n - c0, lc));
-    if constexpr (sizeof(T) == 8)
-      load_rows_async(g, c0, nA, A, c);
-    else if (A32)
-      load_block32(reinterpret_cast<float*>(tab), A32 + c0, c + c0, flags, m, n, nA, ldw, na);
-    else
+    bool ok = true;
+    if constexpr (sizeof(T) == 8) {
+      ok = load_rows_async(g, c0, nA, A, c);
+    } else if (A32) {
+      const int pitch = a32_pitch(n);
+      // one bulk copy when the copy's rows are the tableau's: a single-CTA
+      // LP without phase-I columns, both addresses 16-byte aligned, and the
+      // block within the mbarrier's transaction count
+      const bool whole = c0 == 0 && na == 0 && ldw == pitch &&
+                         ((smem_addr(tab) | (unsigned)reinterpret_cast<uintptr_t>(A32)) & 15u) == 0 &&
+                         (size_t)m * ldw * 4 < (size_t(1) << 20);
+      if (whole)
+        ok = load_block_bulk32(g, A32, c);
+      else
+        load_block32(reinterpret_cast<float*>(tab), A32 + c0, c + c0, flags, m, pitch, nA, ldw,
+                     na);
+    } else {
       load_block(tab, A + c0, c + c0, flags, m, n, nA, ldw, na);
+    }
+    if (cluster_any(!ok)) return false;  // the cluster gives the LP up together
     // The rest of every row: slack slots of negated rows (-1 in their own
     // row), zero padding, and the RHS (|b_i|; 0 in the objective row).
     const int wr = ldw - nA;
@@ -2198,6 +2344,19 @@ struct Solver {
         }
       }
       tab[(size_t)i * ldw + lj] = x;
+    }
+    __syncthreads();
+    return true;
+  }
+
+  // The bulk copies of a tableau load did not complete within the wait
+  // limit: the LP is reported undefined with kInfoLoad.
+  __device__ void abandon(const LpArgs& a, int lp) {
+    if (rank == 0 && threadIdx.x == 0) {
+      a.status[lp] = kUndef;
+      a.obj[lp] = 0.0;
+      if (a.pivots) a.pivots[lp] = -1;
+      if (a.info) a.info[lp] = kInfoLoad | a.info_or;
     }
     __syncthreads();
   }
@@ -2286,7 +2445,7 @@ struct Solver {
       const int lp = ca.order[t];
       const int m = a.m[lp], n = a.n[lp];
       const double* A = a.A + a.offA[lp];
-      const float* A32 = a.A32 ? a.A32 + a.offA[lp] : nullptr;
+      const float* A32 = a.A32 ? a.A32 + a.off32[lp] : nullptr;
       const double* b = a.b + a.offb[lp];
       const double* c = a.c + a.offc[lp];
       // two-phase when any b_i < 0 (the reference's rem list, simplex.cu:574-583)
@@ -2310,7 +2469,7 @@ struct Solver {
       place(L, m);
       const int c0 = rank * g.cw;
       const int lc = max(0, min(g.cw, g.Wc - c0));
-      load(g, c0, lc, A, b, c, A32);
+      load(g, c0, lc, A, b, c, A32, a, lp);
       int pivots = 0, degen = 0, cur = 0, st, info = 0;
       const float* w = a.weight ? a.weight + a.offw[lp] : nullptr;
       // final bases verified (and reported) in FP64: the FP32 tableau, and the
@@ -2339,7 +2498,7 @@ struct Solver {
         if (attempt > 0) {
           info |= kInfoFallback;
           if (CLUSTER) csync();
-          load(g, c0, lc, A, b, c, A32);
+          load(g, c0, lc, A, b, c, A32, a, lp);
           piv_fresh = -1;
           bland = false;
           degen = 0;
@@ -2403,7 +2562,7 @@ struct Solver {
                 // infeasible both ways (or dual simplex stuck): cold solve
                 info |= kInfoFallback;
                 if (CLUSTER) csync();
-                load(g, c0, lc, A, b, c, A32);
+                load(g, c0, lc, A, b, c, A32, a, lp);
                 piv_fresh = -1;
                 bland = false;
                 degen = 0;
