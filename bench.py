@@ -74,6 +74,18 @@ def workload(kind: int, rank: int = 0, world: int = 1):
     return sp.generate(kind, n, seed=sp.DEFAULT_SEED, first=lo, share_family_A=True), count
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# solve_kernel<float> at the default workload (10,000 LPs), from an ncu
+# capture of this bench's timed region (one pass, the full-size launch; the
+# two captured launches read 59.43 / 59.34 MB and wrote 8.43 / 8.10 MB).  The
+# writes are mostly lines the L2 flush between steps left dirty.
+KIND3_SOLVE_DRAM_BYTES = (59431680 + 8429312 + 59341824 + 8103424) / 2
+KIND3_SOLVE_DRAM_SOURCE = ("ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,"
+                           "dram__bytes_write.sum --clock-control none --nvtx --nvtx-include "
+                           "timed_region/ python bench.py --steps 2 --warmup 3 --epochs 4 "
+                           "--no-cpu-baseline (mean of the two solve launches)")
+
+
 def pinned(batch):
     """The same batch with A, b, c in pinned (page-locked) host memory, as the
     end-to-end measurement copies from: numpy views of pinned torch tensors,
@@ -353,7 +365,11 @@ def run_learned(args, rank, world, local, dist=None):
                 "d2h_bytes_per_step": int(total * 16), "ms_per_step": e2e_ms,
                 "call": "blpg_learned_solve (include/blpg.h)"},
         "roofline": {"bound": "smem", "achieved": ach, "peak": smem.value, "unit": "GB/s",
-                     "frac": ach / smem.value, "traffic": None,
+                     "frac": ach / smem.value, "traffic": KIND3_SOLVE_DRAM_BYTES,
+                     "traffic_source": KIND3_SOLVE_DRAM_SOURCE,
+                     "hbm": {"achieved": KIND3_SOLVE_DRAM_BYTES / (ms_solve * 1e-3) / 1e9,
+                             "unit": "GB/s", "note": "DRAM bytes of one solve launch over its "
+                             "CUDA-event time: the inputs are read once per LP"},
                      "kernel": "solve_kernel<float> (FP32 condensed tableau pivots)",
                      "bytes_per_pivot": bytes_per_pivot(m, n, 4),
                      "peak_source": "measured live (blpg_measure_peaks: shared-memory stream probe)",
@@ -394,9 +410,20 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", type=int, default=0, metavar="N",
                     help="small solve of N LPs for ncu captures (see the module docstring)")
+    ap.add_argument("--measure-peaks", action="store_true",
+                    help="print the live shared-memory / FP64 / FP32 peak probes and exit")
     args = ap.parse_args()
     if args.profile_case > 0:
         return run_profile_case(args)
+    if args.measure_peaks:
+        import ctypes as C
+        from simplexprojects_gb300 import _native as N
+        smem, f64, f32 = C.c_double(), C.c_double(), C.c_double()
+        N.check(N.lib().blpg_measure_peaks(0, C.byref(smem), C.byref(f64), C.byref(f32)),
+                "blpg_measure_peaks")
+        print(json.dumps({"smem_gbs": smem.value, "fp64_tflops": f64.value,
+                          "fp32_tflops": f32.value}))
+        return
     args.warmup = max(3, args.warmup)
 
     rank = int(os.environ.get("RANK", 0))
