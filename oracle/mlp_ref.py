@@ -69,6 +69,16 @@ def forward_backward(params, X, Y, d_in_pad, hidden, layers, d_out_pad, d_out,
     return loss, np.concatenate(out)
 
 
+def forward(params, X, d_in_pad, hidden, layers, d_out_pad, emulate_bf16=True):
+    """Logits of rows X (B x d_in_pad), as forward_backward computes them."""
+    r = bf16 if emulate_bf16 else (lambda a: np.asarray(a, dtype=np.float64))
+    Ws, bs = unpack(np.asarray(params), d_in_pad, hidden, layers, d_out_pad)
+    h = r(X)
+    for l in range(layers):
+        h = r(np.maximum(h @ r(Ws[l]).T + bs[l], 0.0))
+    return h @ r(Ws[layers]).T + bs[layers]
+
+
 def init_params(d_in, d_in_pad, hidden, layers, d_out, d_out_pad, seed=0):
     """Small random parameters in the packed layout (padding zero)."""
     rng = np.random.default_rng(seed)

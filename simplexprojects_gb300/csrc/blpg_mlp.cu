@@ -1,8 +1,9 @@
 // The learned warm start's network: a multilayer perceptron that reads an
 // LP's normalised [c; b; family one-hot] and scores every column (n + m of
 // them) for membership in the optimal basis.  Hand-written kernels:
-//   - gemm_bf16_nt: C = A B^T + bias (+ReLU) on the BF16 tensor cores
-//     (mma.sync m16n8k16, FP32 accumulation), A and B K-contiguous;
+//   - gemm_tc_nt: C = A B^T + bias (+ReLU) on the 5th-generation tensor
+//     cores (tcgen05.mma, BF16 operands, FP32 accumulators in TMEM), A and B
+//     K-contiguous;
 //   - the BCE-with-sigmoid gradient, ReLU backward, bias gradient,
 //     transposes with BF16 conversion, and Adam on FP32 master weights;
 //   - feature building from device-resident b, c and the top-m selection
@@ -32,93 +33,238 @@ using bf16 = __nv_bfloat16;
   } while (0)
 
 constexpr int kTile = 64;   // all padded dimensions are multiples of 64
-constexpr int kKStep = 32;
-constexpr int kSPad = 8;    // smem row padding (bf16) against bank conflicts
 
-// C[M x N] = A[M x K] . B[N x K]^T (+ bias[N]) (ReLU); writes FP32 and/or BF16.
-// 128 threads: 4 warps, each a 32x32 sub-tile of the 64x64 block tile.
-__global__ void __launch_bounds__(128) gemm_bf16_nt(const bf16* __restrict__ A,
-                                                    const bf16* __restrict__ B,
-                                                    const float* __restrict__ bias,
-                                                    float* __restrict__ Cf,
-                                                    bf16* __restrict__ Cb, int M, int N, int K,
-                                                    int relu) {
-  __shared__ __align__(16) bf16 As[kTile][kKStep + kSPad];
-  __shared__ __align__(16) bf16 Bs[kTile][kKStep + kSPad];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int m0 = blockIdx.y * kTile, n0 = blockIdx.x * kTile;
-  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
-  for (int k0 = 0; k0 < K; k0 += kKStep) {
-    // 64 rows x 32 bf16 = 64 x 4 chunks of 16 bytes per operand
-    for (int c = tid; c < kTile * 4; c += 128) {
-      const int r = c >> 2, q = (c & 3) * 8;
-      *reinterpret_cast<uint4*>(&As[r][q]) =
-          *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * K + k0 + q);
-      *reinterpret_cast<uint4*>(&Bs[r][q]) =
-          *reinterpret_cast<const uint4*>(B + (size_t)(n0 + r) * K + k0 + q);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < kKStep; kk += 16) {
-      uint32_t af[2][4], bfr[4][2];
-      const int ar = lane >> 2, ac = (lane & 3) * 2;
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int r = wm + i * 16 + ar;
-        af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][kk + ac]);
-        af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + ac]);
-        af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][kk + ac + 8]);
-        af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + ac + 8]);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int nr = wn + j * 8 + ar;
-        bfr[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[nr][kk + ac]);
-        bfr[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[nr][kk + ac + 8]);
-      }
-#pragma unroll
-      for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-          asm volatile(
-              "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-              "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};"
-              : "+f"(acc[i][j][0]), "+f"(acc[i][j][1]), "+f"(acc[i][j][2]), "+f"(acc[i][j][3])
-              : "r"(af[i][0]), "r"(af[i][1]), "r"(af[i][2]), "r"(af[i][3]), "r"(bfr[j][0]),
-                "r"(bfr[j][1]));
-    }
-    __syncthreads();
+// ---------------------------------------------------------------------------
+// C[M x N] = A[M x K] . B[N x K]^T (+ bias[N]) (ReLU), FP32 and/or BF16 out,
+// on the 5th-generation tensor cores: BF16 operands in shared memory, FP32
+// accumulators in tensor memory (TMEM).
+//
+// One CTA of 128 threads per 128 x 128 tile of C (M and N multiples of 64:
+// rows of A and B past the matrix load as zeros, and what they produce is
+// not stored).  K runs in chunks of 64 through three shared-memory stages:
+// all threads stage a chunk of A (128 x 64) and B (128 x 64) by 16-byte
+// cp.async in the canonical K-major layout without swizzle (core matrices of
+// 8 rows x 16 bytes, 128 contiguous bytes; the two core matrices of a
+// 16-wide K step 128 B apart, 8-row groups 1024 B apart, so chunk c of 16
+// bytes -- row group c >> 6, K column group (c >> 3) & 7, row c & 7 -- sits
+// at byte 16 c, and a warp's loads read 8 rows x 64 contiguous bytes), two
+// chunks ahead of the tensor cores.  Thread 0 issues four tcgen05.mma
+// (M = 128, N = 128, K = 16) per chunk and commits them to the stage's
+// mbarrier; a stage is refilled once the commit of the chunk before has
+// arrived.  The accumulator (TMEM lanes 0..127 = rows, 128 columns) is read
+// back by tcgen05.ld, each warp its 32 lanes, and written out through shared
+// memory in row-contiguous pieces.  Every mbarrier wait is
+// bounded; a wait that runs out counts in g_tc_timeouts (checked by the host
+// calls that synchronise), and the CTA still frees its TMEM.
+// ---------------------------------------------------------------------------
+constexpr int kTcM = 128, kTcN = 128, kTcK = 64, kTcStages = 3;
+constexpr int kTcABytes = kTcM * kTcK * 2;  // 16 KB per stage
+constexpr int kTcBBytes = kTcN * kTcK * 2;  // 16 KB per stage
+constexpr int kTcSmem = kTcStages * (kTcABytes + kTcBBytes) + 64;
+constexpr uint32_t kTcCols = kTcN;          // TMEM columns (FP32 accumulators)
+// kind::f16 instruction descriptor: FP32 accumulator (bits 4-5 = 1), BF16 A
+// and B (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at
+// bit 24.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                              ((uint32_t)(kTcM >> 4) << 24);
+constexpr int kTcWaitLimit = 1 << 22;
+__device__ int g_tc_timeouts = 0;
+
+__device__ __forceinline__ uint32_t tc_smem(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+// Shared-memory matrix descriptor: start address, leading-dimension byte
+// offset 128 (the next core matrix along K), stride byte offset 1024 (the
+// next 8-row group), all in 16-byte units; descriptor version 1 (bit 46),
+// no swizzle (layout type 0 in bits 61-63), base offset 0.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16) |
+         ((uint64_t)(1024u >> 4) << 32) | (1ull << 46);
+}
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < kTcWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
   }
-  const int ar = lane >> 2, ac = (lane & 3) * 2;
+  return false;
+}
+
+__global__ void __launch_bounds__(128) gemm_tc_nt(const bf16* __restrict__ A,
+                                                  const bf16* __restrict__ B,
+                                                  const float* __restrict__ bias,
+                                                  float* __restrict__ Cf, bf16* __restrict__ Cb,
+                                                  int M, int N, int K, int relu) {
+  extern __shared__ __align__(1024) unsigned char tc_sm[];
+  unsigned char* sa = tc_sm;                          // A stages
+  unsigned char* sb = tc_sm + kTcStages * kTcABytes;  // B stages
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(sb + kTcStages * kTcBBytes);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + kTcStages);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
+  const int nk = K / kTcK;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     tc_smem(tslot)),
+                 "r"(kTcCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < kTcStages; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&bar[s])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  auto load = [&](int kc, int st) {
+    const int k0 = kc * kTcK;
+    unsigned char* a = sa + st * kTcABytes;
+    unsigned char* b = sb + st * kTcBBytes;
+    for (int c = tid; c < kTcM * 8; c += 128) {
+      const int row = m0 + (c >> 6) * 8 + (c & 7);
+      const int kq = (c >> 3) & 7;
+      if (row < M)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc_smem(a + c * 16)),
+                     "l"(A + (size_t)row * K + k0 + kq * 8)
+                     : "memory");
+      else
+        *reinterpret_cast<uint4*>(a + c * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    for (int c = tid; c < kTcN * 8; c += 128) {
+      const int row = n0 + (c >> 6) * 8 + (c & 7);
+      const int kq = (c >> 3) & 7;
+      if (row < N)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc_smem(b + c * 16)),
+                     "l"(B + (size_t)row * K + k0 + kq * 8)
+                     : "memory");
+      else
+        *reinterpret_cast<uint4*>(b + c * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+
+  // chunks kc and kc + 1 in flight ahead of the tensor cores
+  load(0, 0);
+  if (nk > 1) load(1, 1);
+  uint32_t phases = 0;  // bit s: parity of stage s's next commit
+  bool ok = true;
+  for (int kc = 0; kc < nk; ++kc) {
+    const int st = kc % kTcStages;
+    if (kc + 1 < nk)
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    else
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    // the chunk's shared-memory writes, before the tensor cores read them
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a0 = tc_smem(sa + st * kTcABytes), b0 = tc_smem(sb + st * kTcBBytes);
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int r = m0 + wm + i * 16 + ar + h * 8;
-        const int c = n0 + wn + j * 8 + ac;
-        float v0 = acc[i][j][2 * h], v1 = acc[i][j][2 * h + 1];
-        if (bias) {
-          v0 += bias[c];
-          v1 += bias[c + 1];
-        }
-        if (relu) {
-          v0 = fmaxf(v0, 0.f);
-          v1 = fmaxf(v1, 0.f);
-        }
-        if (Cf) *reinterpret_cast<float2*>(Cf + (size_t)r * N + c) = make_float2(v0, v1);
-        if (Cb)
-          *reinterpret_cast<__nv_bfloat162*>(Cb + (size_t)r * N + c) =
-              __floats2bfloat162_rn(v0, v1);
+      for (int t = 0; t < kTcK / 16; ++t) {
+        const uint64_t da = tc_desc(a0 + 256u * t), db = tc_desc(b0 + 256u * t);
+        const uint32_t acc = (kc > 0 || t > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(kTcIdesc), "r"(acc)
+            : "memory");
       }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              tc_smem(&bar[st]))
+          : "memory");
+    }
+    if (kc + 2 < nk) {
+      // chunk kc + 2 goes into the stage chunk kc - 1 used: its MMAs first
+      const int sn = (kc + 2) % kTcStages;
+      if (kc >= 1) {
+        ok &= tc_wait(tc_smem(&bar[sn]), (phases >> sn) & 1u);
+        phases ^= 1u << sn;
+      }
+      load(kc + 2, sn);
+    }
+  }
+  {  // the last commit covers every MMA issued before it
+    const int st = (nk - 1) % kTcStages;
+    const uint32_t ph = (phases >> st) & 1u;
+    if (!tc_wait(tc_smem(&bar[st]), ph)) {
+      ok = false;
+      tc_wait(tc_smem(&bar[st]), ph);  // let MMAs still running finish before TMEM is freed
+    }
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // Epilogue: each warp reads its 32 rows (TMEM lanes) 16 columns at a time,
+  // adds the bias, applies the ReLU and stages the tile row-major in the
+  // freed operand stages (rows padded by 16 bytes against bank conflicts);
+  // then the CTA writes it out in full 16-byte pieces along rows, so that a
+  // warp's stores cover contiguous bytes.
+  float* tile = reinterpret_cast<float*>(tc_sm);  // 128 x 132 floats < the stages' 96 KB
+  constexpr int ldt = kTcN + 4;
+  const int lrow = warp * 32 + lane;
+  const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+  for (int c0 = 0; c0 < kTcN; c0 += 16) {
+    uint32_t v[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+        "%11, %12, %13, %14, %15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+          "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr + (uint32_t)c0));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    const int col = n0 + c0;
+    float f[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      float x = __uint_as_float(v[j]);
+      if (bias && col < N) x += bias[col + j];  // N is a multiple of 16
+      if (relu) x = fmaxf(x, 0.f);
+      f[j] = x;
+    }
+    float4* d = reinterpret_cast<float4*>(tile + (size_t)lrow * ldt + c0);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) d[j] = make_float4(f[4 * j], f[4 * j + 1], f[4 * j + 2], f[4 * j + 3]);
+  }
+  __syncthreads();
+  if (Cf) {  // 32 pieces of 4 floats per row
+    for (int idx = tid; idx < kTcM * (kTcN / 4); idx += 128) {
+      const int r = idx / (kTcN / 4), q = idx % (kTcN / 4);
+      const int grow = m0 + r, gcol = n0 + 4 * q;
+      if (grow < M && gcol < N)
+        *reinterpret_cast<float4*>(Cf + (size_t)grow * N + gcol) =
+            *reinterpret_cast<const float4*>(tile + (size_t)r * ldt + 4 * q);
+    }
+  }
+  if (Cb) {  // 16 pieces of 8 BF16 per row
+    for (int idx = tid; idx < kTcM * (kTcN / 8); idx += 128) {
+      const int r = idx / (kTcN / 8), q = idx % (kTcN / 8);
+      const int grow = m0 + r, gcol = n0 + 8 * q;
+      if (grow < M && gcol < N) {
+        const float* t = tile + (size_t)r * ldt + 8 * q;
+        __nv_bfloat162 h[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) h[j] = __floats2bfloat162_rn(t[2 * j], t[2 * j + 1]);
+        *reinterpret_cast<uint4*>(Cb + (size_t)grow * N + gcol) = *reinterpret_cast<const uint4*>(h);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols)
+                 : "memory");
+  if (!ok && tid == 0) atomicAdd(&g_tc_timeouts, 1);
 }
 
 // out[c][r] = bf16(in[r][c]) for an R x C row-major input (FP32 or BF16).
@@ -329,11 +475,24 @@ int layer_out(const blpg_mlp* n, int l) { return l == n->layers ? n->d_out_pad :
 
 int32_t gemm(const bf16* A, const bf16* B, const float* bias, float* Cf, bf16* Cb, int M, int N,
              int K, int relu, cudaStream_t s) {
-  if (M % kTile || N % kTile || K % kKStep)
+  if (M % kTile || N % kTile || K % kTcK || M <= 0 || N <= 0 || K <= 0)
     return blpg::fail(BLPG_EINVAL, "gemm: %d x %d x %d not tile-aligned", M, N, K);
-  dim3 grid(N / kTile, M / kTile);
-  gemm_bf16_nt<<<grid, 128, 0, s>>>(A, B, bias, Cf, Cb, M, N, K, relu);
+  MCK(cudaFuncSetAttribute(gemm_tc_nt, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+  dim3 grid((N + kTcN - 1) / kTcN, (M + kTcM - 1) / kTcM);
+  gemm_tc_nt<<<grid, 128, kTcSmem, s>>>(A, B, bias, Cf, Cb, M, N, K, relu);
   MCK(cudaGetLastError());
+  return BLPG_OK;
+}
+
+// Bounded waits of the tensor-core GEMMs that ran out since the last check.
+int32_t check_timeouts() {
+  int t = 0;
+  MCK(cudaMemcpyFromSymbol(&t, g_tc_timeouts, sizeof(int)));
+  if (t) {
+    const int zero = 0;
+    MCK(cudaMemcpyToSymbol(g_tc_timeouts, &zero, sizeof(int)));
+    return blpg::fail(BLPG_ECUDA, "mlp: %d tensor-core GEMM tile(s) timed out", t);
+  }
   return BLPG_OK;
 }
 
@@ -541,6 +700,7 @@ extern "C" int32_t blpg_mlp_gradients(blpg_mlp* n, const float* dX, const float*
   if (rc) return rc;
   if ((rc = backward(n, dY, B, nullptr))) return rc;
   MCK(cudaDeviceSynchronize());
+  if ((rc = check_timeouts())) return rc;
   if (host_grads) MCK(cudaMemcpy(host_grads, n->grads, n->nparams * 4, cudaMemcpyDeviceToHost));
   if (host_loss) MCK(cudaMemcpy(host_loss, n->loss, 4, cudaMemcpyDeviceToHost));
   return BLPG_OK;
@@ -564,6 +724,7 @@ extern "C" int32_t blpg_mlp_train_step(blpg_mlp* n, const float* dX, const float
   if (host_loss) {
     MCK(cudaMemcpyAsync(host_loss, n->loss, 4, cudaMemcpyDeviceToHost, s));
     MCK(cudaStreamSynchronize(s));
+    if ((rc = check_timeouts())) return rc;
   }
   return BLPG_OK;
 }

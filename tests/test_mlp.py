@@ -39,17 +39,20 @@ def test_bf16_rounding():
 
 
 @pytest.mark.gpu
-def test_gpu_gradients_match_oracle(built):
+@pytest.mark.parametrize("rows", [128, 192])
+def test_gpu_gradients_match_oracle(built, rows):
+    """The tensor-core GEMMs (tcgen05, 128-row tiles) in the forward and both
+    backward products; 192 rows leave a half tile in the batch dimension."""
     import torch
     from simplexprojects_gb300.warmstart import MLP
     d_in, hidden, layers, d_out = 100, 128, 3, 70
-    net = MLP(d_in, d_out, hidden, layers, max_batch=128, seed=5)
+    net = MLP(d_in, d_out, hidden, layers, max_batch=rows, seed=5)
     p = net.get_params()
     rng = np.random.default_rng(2)
-    X = np.zeros((128, net.d_in_pad), np.float32)
-    X[:, :d_in] = rng.normal(size=(128, d_in))
-    Y = np.zeros((128, net.d_out_pad), np.float32)
-    Y[:, :d_out] = rng.integers(0, 2, (128, d_out))
+    X = np.zeros((rows, net.d_in_pad), np.float32)
+    X[:, :d_in] = rng.normal(size=(rows, d_in))
+    Y = np.zeros((rows, net.d_out_pad), np.float32)
+    Y[:, :d_out] = rng.integers(0, 2, (rows, d_out))
     g, loss = net.gradients(torch.from_numpy(X).cuda(), torch.from_numpy(Y).cuda())
     lr, gr = mlp_ref.forward_backward(p, X, Y, net.d_in_pad, hidden, layers, net.d_out_pad, d_out)
     assert abs(loss - lr) <= 1e-4 * abs(lr)
@@ -57,6 +60,27 @@ def test_gpu_gradients_match_oracle(built):
     Ws_r, bs_r = mlp_ref.unpack(gr, net.d_in_pad, hidden, layers, net.d_out_pad)
     for a, b in list(zip(Ws_g, Ws_r)) + list(zip(bs_g, bs_r)):
         assert np.linalg.norm(a - b) <= 1e-2 * np.linalg.norm(b) + 1e-9
+
+
+@pytest.mark.gpu
+def test_gpu_forward_matches_oracle(built):
+    """Logits of 320 rows (two full 128-row tiles and a half one) against the
+    oracle's forward pass with the same BF16 roundings."""
+    import torch
+    from simplexprojects_gb300.warmstart import MLP
+    d_in, hidden, layers, d_out, rows = 300, 512, 3, 316, 320
+    net = MLP(d_in, d_out, hidden, layers, max_batch=rows, seed=9)
+    p = net.get_params()
+    rng = np.random.default_rng(4)
+    X = np.zeros((rows, net.d_in_pad), np.float32)
+    X[:, :d_in] = rng.normal(size=(rows, d_in))
+    out = torch.zeros((rows, net.d_out_pad), dtype=torch.float32, device="cuda")
+    net.predict(torch.from_numpy(X).cuda(), out)
+    torch.cuda.synchronize()
+    z = mlp_ref.forward(p, X, net.d_in_pad, hidden, layers, net.d_out_pad)
+    got = out.cpu().numpy()
+    assert np.linalg.norm(got - z) <= 2e-3 * np.linalg.norm(z)
+    assert np.abs(got - z).max() <= 2e-2 * np.abs(z).max()
 
 
 @pytest.mark.gpu
