@@ -7,9 +7,10 @@
 // otherwise chain by hand (blpg_features, blpg_mlp_predict,
 // blpg_price_weights, blpg_plan_execute_weighted).
 //
-// Everything is enqueued on one stream in that order; host arrays in pinned
-// memory make the uploads and downloads asynchronous to the host until the
-// final synchronisation.
+// Everything is enqueued on one stream in that order, except A's upload,
+// which runs on a second stream beside the network and which the solve
+// waits for; host arrays in pinned memory make the uploads and downloads
+// asynchronous to the host until the final synchronisation.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,6 +27,8 @@ struct blpg_learned {
   int d_in_pad = 0, d_out_pad = 0, rows = 0;
   int64_t extA = 0, extb = 0, extc = 0, extw = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t stream_a = nullptr;  // A's upload, beside the network
+  cudaEvent_t a_landed = nullptr;
   // device buffers
   double *A = nullptr, *b = nullptr, *c = nullptr, *obj = nullptr, *x = nullptr;
   int32_t *fam = nullptr, *dm = nullptr, *dn = nullptr, *st = nullptr, *piv = nullptr,
@@ -50,6 +53,8 @@ void release(blpg_learned* L) {
   void* bufs[] = {L->A, L->b, L->c, L->obj, L->x, L->fam, L->dm, L->dn, L->st, L->piv, L->info,
                   L->offb, L->offc, L->offw, L->mean, L->std_, L->X, L->logits, L->w};
   for (void* p : bufs) cudaFree(p);
+  if (L->a_landed) cudaEventDestroy(L->a_landed);
+  if (L->stream_a) cudaStreamDestroy(L->stream_a);
   if (L->stream) cudaStreamDestroy(L->stream);
 }
 
@@ -118,6 +123,8 @@ extern "C" int32_t blpg_learned_create(blpg_mlp* mlp, int32_t families, const fl
   }
   L->extw = (int64_t)N * (n + m);
   cudaError_t e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L->stream_a, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L->a_landed, cudaEventDisableTiming);
   if (e != cudaSuccess) return bail(fail(BLPG_ECUDA, "blpg_learned_create: stream"));
   const size_t F = (size_t)families * (n + m);
 #define LMAL(p, bytes)                                                              \
@@ -171,7 +178,11 @@ extern "C" int32_t blpg_learned_solve(blpg_learned* L, const blpg_batch* bt,
     return fail(BLPG_EINVAL, "blpg_learned_solve: the batch is not the one the solver was made for");
   const int N = L->count;
   cudaStream_t s = L->stream;
-  LCK(cudaMemcpyAsync(L->A, bt->A, sizeof(double) * (size_t)L->extA, cudaMemcpyHostToDevice, s));
+  // A is read only by the solve: its upload runs on a second stream while b,
+  // c and the family ids upload and the network runs
+  LCK(cudaMemcpyAsync(L->A, bt->A, sizeof(double) * (size_t)L->extA, cudaMemcpyHostToDevice,
+                      L->stream_a));
+  LCK(cudaEventRecord(L->a_landed, L->stream_a));
   LCK(cudaMemcpyAsync(L->b, bt->b, sizeof(double) * (size_t)L->extb, cudaMemcpyHostToDevice, s));
   LCK(cudaMemcpyAsync(L->c, bt->c, sizeof(double) * (size_t)L->extc, cudaMemcpyHostToDevice, s));
   LCK(cudaMemcpyAsync(L->fam, host_family, sizeof(int32_t) * N, cudaMemcpyHostToDevice, s));
@@ -185,6 +196,7 @@ extern "C" int32_t blpg_learned_solve(blpg_learned* L, const blpg_batch* bt,
     return rc;
   blpg_result dres{L->st, L->obj, out->x ? L->x : nullptr, out->pivots ? L->piv : nullptr,
                    nullptr, out->info ? L->info : nullptr};
+  LCK(cudaStreamWaitEvent(s, L->a_landed, 0));
   if ((rc = blpg_plan_execute_weighted(L->plan, L->A, L->b, L->c, nullptr, L->w, &dres, s)))
     return rc;
   LCK(cudaMemcpyAsync(out->status, L->st, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, s));
@@ -203,6 +215,7 @@ extern "C" int32_t blpg_learned_solve(blpg_learned* L, const blpg_batch* bt,
 extern "C" void blpg_learned_destroy(blpg_learned* L) {
   if (!L) return;
   if (L->stream) cudaStreamSynchronize(L->stream);
+  if (L->stream_a) cudaStreamSynchronize(L->stream_a);
   release(L);
   delete L;
 }
