@@ -101,8 +101,11 @@ typedef struct blpg_options {
   int32_t bland_after;     /* consecutive degenerate pivots before Bland's
                               rule takes over for the rest of the LP; 0 = 64 */
   int32_t refactor_period; /* FP32 only: FP64 refresh of x_B, the duals and
-                              the reduced costs every k pivots; 0 = only at
-                              termination (always done there) */
+                              the reduced costs every k pivots (always done
+                              at termination too); 0 = the tuning table's
+                              period ("fp32_refresh_period"; the GB300 table
+                              has 0: termination only); < 0 = termination
+                              only */
   double opt_tol;          /* reduced-cost tolerance; 0 = 1e-9 (FP64) / 1e-5 */
   double piv_tol;          /* pivot tolerance;       0 = 1e-7 (FP64) / 1e-5 */
   const int32_t* basis_hint; /* nullable warm start (host memory for

@@ -23,7 +23,8 @@ lays entries over the compiled-in one and ``reset()`` restores it.
     python -m simplexprojects_gb300.autotune --out simplexprojects_gb300/tuning/gb300.json
 
 tunes FP32 steepest edge on workloads 0-4 and FP64 Dantzig on workloads 1, 2
-and 4.
+and 4, then the FP32 refresh period (an FP64 refresh every k pivots, or only
+at termination) on workloads 1-4.
 """
 from __future__ import annotations
 
@@ -151,6 +152,33 @@ def tune(batches: dict, precision: str = "fp32", pricing: str = "dantzig",
     return table
 
 
+def tune_refresh(batches: dict, periods=(0, 16, 32, 64), steps: int = 5, log=print) -> dict:
+    """The FP32 refresh period: FP32 steepest edge on each workload with an
+    FP64 refresh every k pivots (0: at termination only), statuses checked;
+    the period with the lowest sum of time over each workload's best."""
+    from .solver import DeviceBatch
+    rows, ref = [], {}
+    for k in periods:
+        times, same = {}, True
+        for name, batch in batches.items():
+            db = DeviceBatch(batch, "fp32", pricing="steepest", refactor_period=k if k > 0 else -1)
+            times[name] = _time(db, steps)
+            st = db.result().status
+            ref.setdefault(name, st)
+            same &= bool(np.array_equal(st, ref[name]))
+            db.plan.close()
+        rows.append(dict(period=k, ms=times, statuses_equal=same))
+        if log:
+            log(f"fp32 refresh every {k or 'end'}: " +
+                ", ".join(f"{n} {t:8.3f} ms" for n, t in times.items()))
+    ok = [r for r in rows if r["statuses_equal"]]
+    best_ms = {n: min(r["ms"][n] for r in ok) for n in batches}
+    for r in ok:
+        r["score"] = sum(r["ms"][n] / best_ms[n] for n in batches)
+    best = min(ok, key=lambda r: r["score"])
+    return {"fp32_refresh_period": best["period"], "measured": {"fp32_refresh_period": rows}}
+
+
 def load(path: str) -> dict:
     """Apply a tuning table to the library (later plans and solves use it)."""
     table = json.loads(Path(path).read_text())
@@ -177,19 +205,31 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default="tuning.json")
     ap.add_argument("--waves", type=int, default=4)
+    ap.add_argument("--only", choices=["classes", "refresh"], default=None,
+                    help="tune one part and merge it into --merge (default: both)")
+    ap.add_argument("--merge", default=None, help="existing table to update")
     args = ap.parse_args()
     sizes = {0: 1024, 1: 10_000, 2: 2048, 3: 10_000, 4: 20_000}
     work = {k: generate(k, n, share_family_A=k in (3, 4)) for k, n in sizes.items()}
-    runs = [("fp32", "steepest", (0, 1, 2, 3, 4)), ("fp64", "dantzig", (1, 2, 4))]
     table = {"measured": {}}
-    for prec, pricing, kinds in runs:
-        tuned = tune({f"kind{k}": work[k] for k in kinds}, prec, pricing=pricing,
-                     waves=args.waves, base={})
-        table["measured"].update({f"{k}_{pricing}": v for k, v in tuned.pop("measured").items()})
+    if args.merge:
+        table = json.loads(Path(args.merge).read_text())
+        table.setdefault("measured", {})
+    if args.only in (None, "classes"):
+        runs = [("fp32", "steepest", (0, 1, 2, 3, 4)), ("fp64", "dantzig", (1, 2, 4))]
+        for prec, pricing, kinds in runs:
+            tuned = tune({f"kind{k}": work[k] for k in kinds}, prec, pricing=pricing,
+                         waves=args.waves, base={})
+            table["measured"].update({f"{k}_{pricing}": v for k, v in tuned.pop("measured").items()})
+            table.update(tuned)
+        table["how"] = ("python -m simplexprojects_gb300.autotune: per class key, the class's LPs "
+                        "of each workload repeated to %d waves of the GPU; the lowest sum of time "
+                        "over each workload's best time; the FP32 refresh period on workloads 1-4 "
+                        "the same way" % args.waves)
+    if args.only in (None, "refresh"):
+        tuned = tune_refresh({f"kind{k}": work[k] for k in (1, 2, 3, 4)})
+        table["measured"].update(tuned.pop("measured"))
         table.update(tuned)
-    table["how"] = ("python -m simplexprojects_gb300.autotune: per class key, the class's LPs of "
-                    "each workload repeated to %d waves of the GPU; the lowest sum of time over "
-                    "each workload's best time" % args.waves)
     Path(args.out).parent.mkdir(parents=True, exist_ok=True)
     Path(args.out).write_text(json.dumps(table, indent=1))
     print(json.dumps({k: v for k, v in table.items() if k not in ("measured", "how")}))

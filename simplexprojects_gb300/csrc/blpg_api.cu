@@ -610,6 +610,8 @@ static void parse_tuning_locked(const char* json) {
         g_tuning.threads[{prec * 16 + 15, 1}] = val;
       else if (std::strcmp(rest, "ctas") == 0 && val > 0)
         g_tuning.threads[{prec * 16 + 14, 2}] = val;
+      else if (std::strcmp(rest, "refresh_period") == 0 && val >= 0)
+        g_tuning.threads[{prec * 16 + 11, 3}] = val;
     } else if (key == "overlap_mb" && val > 0) {
       g_tuning.threads[{-1, 1}] = val;
     } else if (key == "device_budget_mb" && val > 0) {
@@ -869,7 +871,12 @@ extern "C" int32_t blpg_plan_execute_weighted(blpg_plan* p, const double* dA, co
   a.deg_tol = fp32 ? 1e-7 : 1e-12;
   a.harris = p->opt.ratio_rule == 1 ? 0 : 1;
   a.ptol = fp32 ? 1e-7 : 1e-9;
-  a.refresh_period = p->opt.refactor_period > 0 ? p->opt.refactor_period : 0;
+  // 0: the tuning table's period ("fpXX_refresh_period", 0 = termination
+  // only); negative: termination only
+  a.refresh_period = p->opt.refactor_period > 0
+                         ? p->opt.refactor_period
+                         : (p->opt.refactor_period == 0 ? tuning_value(p->precision * 16 + 11, 3, 0)
+                                                        : 0);
   a.hint = basis_hint;
   a.info = out->info;
   a.warm_mode = p->opt.warm_mode == 0 ? 1 : (p->opt.warm_mode == 2 ? 0 : 1);
