@@ -1,6 +1,6 @@
 """Exact rational dense simplex (fractions.Fraction) — TEST INFRASTRUCTURE ONLY.
 
-A small exact judge that travels to any host (glp_exact's library is x86
+A small exact arbiter that travels to any host (glp_exact's library is x86
 only).  Textbook two-phase tableau simplex with Bland's rule, so it cannot
 cycle; meant for LPs with a few dozen rows.  It follows the same method as
 the reference (simplex.cu, tableau from the slack basis, phase I with

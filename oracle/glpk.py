@@ -4,7 +4,7 @@ The reference judges its GPU results against GLPK 4.45 (ReadMe:26): each LP
 becomes one problem object with rows ``GLP_UP`` (a_i x <= b_i), columns
 ``GLP_LO`` (x >= 0), the objective set per LP and ``glp_simplex`` run with
 default parameters (glpk_lp_solver.cpp:243-286, :435-454, GPU_Tester.cu:154-164).
-``glp_exact`` (GMP rationals, same library) is the exact judge.
+``glp_exact`` (GMP rationals, same library) is the exact arbiter.
 
 GLPK is third-party and not in the reference's sources: only its prebuilt
 x86-64 shared library ships (lib/libglpk.so.0.30.0, version string "4.45").
