@@ -1950,7 +1950,8 @@ struct Solver {
         }
         __syncthreads();
         // dy_k = sum_i s_i Binv_ik in FP32: a basic slack k in row i takes
-        // s_i, a nonbasic one sums its stored column (one thread per slack)
+        // s_i, a nonbasic one sums its stored column over the structural
+        // basics' rows (one thread per slack)
         for (int kb = tid & ~31; kb < m; kb += nt) {  // warp-uniform trip count
           const int k = kb + lane;
           float acc = 0.f;
@@ -1959,15 +1960,21 @@ struct Solver {
             if (sv < 0) {
               acc = rf[-1 - sv];
             } else {
+              // s_i is 0 on the rows of basic slacks (-y_k, and y_k is 0
+              // there), so the sum runs over the structural basics' rows
               float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f;
-              int i = 0;
-              for (; i + 4 <= m; i += 4) {
-                q0 = fmaf(rf[i], (float)*elem(g, i, sv), q0);
-                q1 = fmaf(rf[i + 1], (float)*elem(g, i + 1, sv), q1);
-                q2 = fmaf(rf[i + 2], (float)*elem(g, i + 2, sv), q2);
-                q3 = fmaf(rf[i + 3], (float)*elem(g, i + 3, sv), q3);
+              int t = 0;
+              for (; t + 4 <= ns; t += 4) {
+                const int i0 = slist[t], i1 = slist[t + 1], i2 = slist[t + 2], i3 = slist[t + 3];
+                q0 = fmaf(rf[i0], (float)*elem(g, i0, sv), q0);
+                q1 = fmaf(rf[i1], (float)*elem(g, i1, sv), q1);
+                q2 = fmaf(rf[i2], (float)*elem(g, i2, sv), q2);
+                q3 = fmaf(rf[i3], (float)*elem(g, i3, sv), q3);
               }
-              for (; i < m; ++i) q0 = fmaf(rf[i], (float)*elem(g, i, sv), q0);
+              for (; t < ns; ++t) {
+                const int i0 = slist[t];
+                q0 = fmaf(rf[i0], (float)*elem(g, i0, sv), q0);
+              }
               acc = (q0 + q1) + (q2 + q3);
             }
             yr[k] += (double)acc;
