@@ -1780,7 +1780,6 @@ struct Solver {
     if (CLUSTER) csync();
     int ok = 0;
     if (rank == 0) {
-      double* res = reinterpret_cast<double*>(col0);   // col0|col1: m doubles
       double* part = reinterpret_cast<double*>(redP);  // 192 doubles of partial sums
       // Structural basics as a list of rows in row order (flags[], its
       // warm-start use is over by now); nonbasic slacks as a list of slack
@@ -1824,17 +1823,38 @@ struct Solver {
       }
       __syncthreads();
       const int ns = wcount[nch], nn = wcount[64 + nch];
-      // Largest |correction| and |value| of a refinement step: positive
-      // floats order like their bit patterns, so a shared atomicMax works.
-      unsigned* mx = &sh->aux.w2;  // [0] max |correction|, [1] max |value|
+      // x_B and the duals are refined side by side, pass for pass (they are
+      // independent: x_B from b, y from c), so that each pass's residuals
+      // and corrections of both are in flight together; each stops at its
+      // own convergence, and every element is computed exactly as it would
+      // be alone.  Residuals rounded to FP32: rfx (rf) for x_B, rfy (col0)
+      // for y.  Largest |correction| and |value| of a step: positive floats
+      // order like their bit patterns, so a shared atomicMax works.
+      float* rfx = rf;
+      float* rfy = reinterpret_cast<float*>(col0);
+      unsigned* mx = &sh->aux.w2;                          // x: [0] |correction|, [1] |value|
+      unsigned* my = reinterpret_cast<unsigned*>(&sh->pad0);  // y: the same
       for (int i = tid; i < m; i += nt) xr[i] = (double)tab[(size_t)i * g.ldw + g.cw];
-      bool xconv = false;
+      // initial duals: y_k = d of slack k (0 when the slack is basic)
+      for (int k = tid; k < m; k += nt) {
+        const int sv = vpos[n + k];
+        yr[k] = sv >= 0 ? (double)*elem(g, m, sv) : 0.0;
+      }
+      // y_k is exactly 0 for every basic slack k (it starts at 0 and its
+      // correction is its own residual, -y_k), so the sums over k below run
+      // over the nonbasic slacks (nlist, nn of them) only.  The range of each
+      // structural basic's column sum is split in P parts (partial sums in
+      // `part`, 192 doubles), combined in a fixed order; P = 1 above 96
+      // basics
+      const int P = (ns > 0 && ns <= 96) ? min(4, 192 / ns) : 1;
+      const int kc = ceil_div(nn, P);
+      bool xconv = false, yconv = false;
       for (int it = 0; it < kRefineIters; ++it) {
-        if (tid == 0) mx[0] = mx[1] = 0u;
+        if (tid == 0) mx[0] = mx[1] = my[0] = my[1] = 0u;
         __syncthreads();
         // r_k = b_k - sum_t A_k,col_t x_t - x_(slack k, when basic): one
         // thread per row, four interleaved partial sums over the basics
-        for (int k = tid; k < m; k += nt) {
+        for (int k = tid; k < m && !xconv; k += nt) {
           const double* Ak = A + (size_t)k * n;
           double p0 = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;
           int t = 0;
@@ -1852,68 +1872,11 @@ struct Solver {
           double r = b[k] - ((p0 + p1) + (p2 + p3));
           const int sv = vpos[n + k];
           if (sv < 0) r = r - xr[-1 - sv];
-          res[k] = r;
-          rf[k] = (float)r;
+          rfx[k] = (float)r;
         }
-        __syncthreads();
-        // dx_i = sum_k Binv_ik r_k in FP32: one thread per row i over the
-        // nonbasic slacks' columns, plus r_k when row i holds basic slack k
-        for (int ib = tid & ~31; ib < m; ib += nt) {  // warp-uniform trip count
-          const int i = ib + lane;
-          float acc = 0.f;
-          if (i < m) {
-            float q0 = 0.f, q1 = 0.f;
-            int u = 0;
-            for (; u + 2 <= nn; u += 2) {
-              const int k0 = nlist[u], k1 = nlist[u + 1];
-              q0 = fmaf((float)*elem(g, i, vpos[n + k0]), rf[k0], q0);
-              q1 = fmaf((float)*elem(g, i, vpos[n + k1]), rf[k1], q1);
-            }
-            if (u < nn) {
-              const int k0 = nlist[u];
-              q0 = fmaf((float)*elem(g, i, vpos[n + k0]), rf[k0], q0);
-            }
-            acc = q0 + q1;
-            const int bi = basis[i];
-            if (bi >= n && bi < n + m) acc = acc + rf[bi - n];
-            xr[i] += (double)acc;
-          }
-          const unsigned c0m = __reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(acc)));
-          const unsigned c1m =
-              __reduce_max_sync(0xffffffffu, i < m ? __float_as_uint(fabsf((float)xr[i])) : 0u);
-          if (lane == 0) {
-            atomicMax(&mx[0], c0m);
-            atomicMax(&mx[1], c1m);
-          }
-        }
-        __syncthreads();
-        if (__uint_as_float(mx[0]) <= 1e-10f * fmaxf(1.f, __uint_as_float(mx[1]))) {
-          xconv = true;
-          break;
-        }
-        __syncthreads();
-      }
-      __syncthreads();
-      // initial duals: y_k = d of slack k (0 when the slack is basic)
-      for (int k = tid; k < m; k += nt) {
-        const int sv = vpos[n + k];
-        yr[k] = sv >= 0 ? (double)*elem(g, m, sv) : 0.0;
-      }
-      // y_k is exactly 0 for every basic slack k (it starts at 0 and its
-      // correction is its own residual, -y_k), so the sums over k below run
-      // over the nonbasic slacks (nlist, nn of them) only.  The range of each
-      // structural basic's column sum is split in P parts (partial sums in
-      // `part`, 192 doubles), combined in a fixed order; P = 1 above 96
-      // basics
-      const int P = (ns > 0 && ns <= 96) ? min(4, 192 / ns) : 1;
-      const int kc = ceil_div(nn, P);
-      bool yconv = false;
-      for (int it = 0; it < kRefineIters; ++it) {
-        if (tid == 0) mx[0] = mx[1] = 0u;
-        __syncthreads();
         // s_i = cB_i - (B^T y)_i: structural basic in row i with column col:
         // c_col - sum_k A_k,col y_k; basic slack k: -y_k
-        for (int w = tid; w < ns * P; w += nt) {
+        for (int w = tid; w < ns * P && !yconv; w += nt) {
           const int t = w % ns, pp = w / ns;
           const int col = basis[slist[t]];
           const int u0 = pp * kc, u1 = min(nn, u0 + kc);
@@ -1925,40 +1888,65 @@ struct Solver {
             p1 = fma(__ldg(A + (size_t)k2 * n + col), yr[k2], p1);
           }
           if (u < u1) p0 = fma(__ldg(A + (size_t)nlist[u] * n + col), yr[nlist[u]], p0);
-          if (P == 1) {
-            const double sv = c[col] - (p0 + p1);
-            res[slist[t]] = sv;
-            rf[slist[t]] = (float)sv;
-          } else
+          if (P == 1)
+            rfy[slist[t]] = (float)(c[col] - (p0 + p1));
+          else
             part[pp * ns + t] = p0 + p1;
         }
-        for (int i = tid; i < m; i += nt) {
+        for (int i = tid; i < m && !yconv; i += nt) {
           const int bi = basis[i];
-          if (bi >= n) {
-            const double sv = bi < n + m ? -yr[bi - n] : 0.0;
-            res[i] = sv;
-            rf[i] = (float)sv;
+          if (bi >= n) rfy[i] = (float)(bi < n + m ? -yr[bi - n] : 0.0);
+        }
+        __syncthreads();
+        if (!yconv && P > 1) {
+          for (int t = tid; t < ns; t += nt) {
+            double sum = part[t];
+            for (int pp = 1; pp < P; ++pp) sum += part[pp * ns + t];
+            const int i = slist[t];
+            rfy[i] = (float)(c[basis[i]] - sum);
+          }
+          __syncthreads();
+        }
+        // dx_i = sum_k Binv_ik r_k in FP32: one thread per row i over the
+        // nonbasic slacks' columns, plus r_k when row i holds basic slack k
+        for (int ib = tid & ~31; ib < m && !xconv; ib += nt) {  // warp-uniform trip count
+          const int i = ib + lane;
+          float acc = 0.f;
+          if (i < m) {
+            float q0 = 0.f, q1 = 0.f;
+            int u = 0;
+            for (; u + 2 <= nn; u += 2) {
+              const int k0 = nlist[u], k1 = nlist[u + 1];
+              q0 = fmaf((float)*elem(g, i, vpos[n + k0]), rfx[k0], q0);
+              q1 = fmaf((float)*elem(g, i, vpos[n + k1]), rfx[k1], q1);
+            }
+            if (u < nn) {
+              const int k0 = nlist[u];
+              q0 = fmaf((float)*elem(g, i, vpos[n + k0]), rfx[k0], q0);
+            }
+            acc = q0 + q1;
+            const int bi = basis[i];
+            if (bi >= n && bi < n + m) acc = acc + rfx[bi - n];
+            xr[i] += (double)acc;
+          }
+          const unsigned c0m = __reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(acc)));
+          const unsigned c1m =
+              __reduce_max_sync(0xffffffffu, i < m ? __float_as_uint(fabsf((float)xr[i])) : 0u);
+          if (lane == 0) {
+            atomicMax(&mx[0], c0m);
+            atomicMax(&mx[1], c1m);
           }
         }
-        __syncthreads();
-        for (int t = tid; t < ns && P > 1; t += nt) {
-          double sum = part[t];
-          for (int pp = 1; pp < P; ++pp) sum += part[pp * ns + t];
-          const int i = slist[t];
-          res[i] = c[basis[i]] - sum;
-          rf[i] = (float)res[i];
-        }
-        __syncthreads();
         // dy_k = sum_i s_i Binv_ik in FP32: a basic slack k in row i takes
         // s_i, a nonbasic one sums its stored column over the structural
         // basics' rows (one thread per slack)
-        for (int kb = tid & ~31; kb < m; kb += nt) {  // warp-uniform trip count
+        for (int kb = tid & ~31; kb < m && !yconv; kb += nt) {  // warp-uniform trip count
           const int k = kb + lane;
           float acc = 0.f;
           if (k < m) {
             const int sv = vpos[n + k];
             if (sv < 0) {
-              acc = rf[-1 - sv];
+              acc = rfy[-1 - sv];
             } else {
               // s_i is 0 on the rows of basic slacks (-y_k, and y_k is 0
               // there), so the sum runs over the structural basics' rows
@@ -1966,14 +1954,14 @@ struct Solver {
               int t = 0;
               for (; t + 4 <= ns; t += 4) {
                 const int i0 = slist[t], i1 = slist[t + 1], i2 = slist[t + 2], i3 = slist[t + 3];
-                q0 = fmaf(rf[i0], (float)*elem(g, i0, sv), q0);
-                q1 = fmaf(rf[i1], (float)*elem(g, i1, sv), q1);
-                q2 = fmaf(rf[i2], (float)*elem(g, i2, sv), q2);
-                q3 = fmaf(rf[i3], (float)*elem(g, i3, sv), q3);
+                q0 = fmaf(rfy[i0], (float)*elem(g, i0, sv), q0);
+                q1 = fmaf(rfy[i1], (float)*elem(g, i1, sv), q1);
+                q2 = fmaf(rfy[i2], (float)*elem(g, i2, sv), q2);
+                q3 = fmaf(rfy[i3], (float)*elem(g, i3, sv), q3);
               }
               for (; t < ns; ++t) {
                 const int i0 = slist[t];
-                q0 = fmaf(rf[i0], (float)*elem(g, i0, sv), q0);
+                q0 = fmaf(rfy[i0], (float)*elem(g, i0, sv), q0);
               }
               acc = (q0 + q1) + (q2 + q3);
             }
@@ -1983,15 +1971,16 @@ struct Solver {
           const unsigned c1m =
               __reduce_max_sync(0xffffffffu, k < m ? __float_as_uint(fabsf((float)yr[k])) : 0u);
           if (lane == 0) {
-            atomicMax(&mx[0], c0m);
-            atomicMax(&mx[1], c1m);
+            atomicMax(&my[0], c0m);
+            atomicMax(&my[1], c1m);
           }
         }
         __syncthreads();
-        if (__uint_as_float(mx[0]) <= 1e-10f * fmaxf(1.f, __uint_as_float(mx[1]))) {
+        if (!xconv && __uint_as_float(mx[0]) <= 1e-10f * fmaxf(1.f, __uint_as_float(mx[1])))
+          xconv = true;
+        if (!yconv && __uint_as_float(my[0]) <= 1e-10f * fmaxf(1.f, __uint_as_float(my[1])))
           yconv = true;
-          break;
-        }
+        if (xconv && yconv) break;
         __syncthreads();
       }
       // Reduced costs d_j = y^T a_j - c_j of the nonbasic structural
