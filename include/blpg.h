@@ -219,8 +219,10 @@ int32_t blpg_solve_batch(const blpg_batch* batch, const blpg_options* opt,
  * as many chunks as that budget needs, taking turns in two device regions
  * (the reference's tester splits such batches by device memory on the host,
  * GPU_Tester.cu:194-238).  Results are the same as one plan's.  Tuning-table
- * keys "overlap_mb" and "device_budget_mb" change the two thresholds and
- * "overlap_chunks" the chunk count.
+ * keys "overlap_mb" and "device_budget_mb" change the two thresholds,
+ * "overlap_chunks" the chunk count and "overlap_order" the enqueue order
+ * (0: all uploads first from pinned memory, alternating from pageable; 1:
+ * always alternating; 2: always uploads first).
  * blpg_solve_batch_chunks returns how many chunks the last call used
  * (1: one plan). */
 int32_t blpg_solve_batch_chunks(void);

@@ -618,6 +618,8 @@ static void parse_tuning_locked(const char* json) {
       g_tuning.threads[{-1, 2}] = val;
     } else if (key == "overlap_chunks" && val > 1) {
       g_tuning.threads[{-1, 3}] = val;
+    } else if (key == "overlap_order" && val >= 0 && val <= 2) {
+      g_tuning.threads[{-1, 4}] = val;
     }
     s = colon + 1;
   }
@@ -1384,7 +1386,8 @@ static int32_t solve_chunked(const blpg_batch* bt, const blpg_options& opt, blpg
   cudaGetLastError();  // a pageable pointer may leave an error on older runtimes
   const int lag = ring ? ring - 1 : chunks - 1;
   int32_t rc = BLPG_OK;
-  if (!ring && pinned) {
+  const int order = tuning_value(-1, 4, 0);  // 1: alternate, 2: uploads first, 0: by memory kind
+  if (!ring && (order == 2 || (order == 0 && pinned))) {
     for (int ch = 0; ch < chunks; ++ch)
       if ((rc = upload(ch))) return rc;
     for (int ch = 0; ch < chunks; ++ch)
