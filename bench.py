@@ -77,9 +77,9 @@ def workload(kind: int, rank: int = 0, world: int = 1):
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
 # solve_kernel<float> at the default workload (10,000 LPs), from an ncu
 # capture of this bench's timed region (one pass, the full-size launch; the
-# two captured launches read 59.82 / 59.67 MB and wrote 9.73 / 9.15 MB).  The
+# two captured launches read 59.24 / 59.12 MB and wrote 6.98 / 6.52 MB).  The
 # writes are mostly lines the L2 flush between steps left dirty.
-KIND3_SOLVE_DRAM_BYTES = (59818240 + 9729536 + 59673344 + 9149184) / 2
+KIND3_SOLVE_DRAM_BYTES = (59242240 + 6981120 + 59117824 + 6521856) / 2
 KIND3_SOLVE_DRAM_SOURCE = ("ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,"
                            "dram__bytes_write.sum --clock-control none --nvtx --nvtx-include "
                            "timed_region/ python bench.py --steps 2 --warmup 3 --epochs 4 "
