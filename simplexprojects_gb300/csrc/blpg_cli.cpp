@@ -13,9 +13,7 @@
 //           answer in this mode and exits, GPU_Tester.cu:67-79).
 // The batch is solved `average`+1 times; the first run is warm-up and the
 // rest are averaged (GPU_Tester.cu:242-262).  Batches larger than what fits
-// the device's free memory are solved in chunks (GPU_Tester.cu:194-238).
-#include <cuda_runtime.h>
-
+// the device's free memory are split by the library (GPU_Tester.cu:194-238).
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -91,36 +89,27 @@ int main(int argc, char** argv) {
   blpg::matrix<double> C(batch, A.size2());
   for (int i = 0; i < batch; ++i)
     for (size_t j = 0; j < A.size2(); ++j) C(i, j) = minimise ? -c[j] : c[j];
-  // chunking by free device memory, as the reference's multiple-batch path
-  size_t free_b = 0, total_b = 0;
-  cudaMemGetInfo(&free_b, &total_b);
-  const size_t per_lp = 64 + 8 * (A.size2() + 4);
-  const size_t cap = free_b > (1u << 28) ? (free_b - (1u << 28)) / per_lp : 1;
-  const int chunk = (int)std::max<size_t>(1, std::min<size_t>(cap, (size_t)batch));
+  // one call per run: blpg_solve_batch pipelines a large batch in chunks and
+  // splits one that does not fit the device itself (the reference's
+  // multiple-batch path, GPU_Tester.cu:194-238, 284-354)
   std::vector<double> result(batch);
   std::vector<int> status(batch);
   double sum = 0.0;
   for (int it = 0; it <= avg; ++it) {
     const auto t0 = std::chrono::steady_clock::now();
-    for (int k0 = 0; k0 < batch; k0 += chunk) {
-      const int k = std::min(chunk, batch - k0);
-      blpg::matrix<double> Ck(k, A.size2());
-      for (int i = 0; i < k; ++i)
-        for (size_t j = 0; j < A.size2(); ++j) Ck(i, j) = C(k0 + i, j);
-      blpg::Simplex s(k, chunk < batch ? 1 : 0);
-      s.setConstratint(A, b);
-      try {
-        s.ComputeLP(Ck, streams);
-      } catch (const std::exception& e) {
-        std::fprintf(stderr, "%s\n", e.what());
-        return 1;
-      }
-      auto r = s.getResultAll();
-      auto st = s.getStatusAll();
-      for (int i = 0; i < k; ++i) {
-        result[k0 + i] = r[i];
-        status[k0 + i] = st[i];
-      }
+    blpg::Simplex s(batch, 0);
+    s.setConstratint(A, b);
+    try {
+      s.ComputeLP(C, streams);
+    } catch (const std::exception& e) {
+      std::fprintf(stderr, "%s\n", e.what());
+      return 1;
+    }
+    auto r = s.getResultAll();
+    auto st = s.getStatusAll();
+    for (int i = 0; i < batch; ++i) {
+      result[i] = r[i];
+      status[i] = st[i];
     }
     const double sec =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
