@@ -226,6 +226,10 @@ int32_t blpg_solve_batch(const blpg_batch* batch, const blpg_options* opt,
  * blpg_solve_batch_chunks returns how many chunks the last call used
  * (1: one plan). */
 int32_t blpg_solve_batch_chunks(void);
+/* blpg_solve_batch keeps its last plans and device buffers for the next call
+ * with the same shapes (grow-only); this frees them (the next call rebuilds
+ * what it needs).  Safe to call at any time between solves. */
+int32_t blpg_release_workspace(void);
 
 /* Plans: the size classes, work queues, device scratch and CUDA graph for
  * one batch shape, built once and replayed.  blpg_plan_create reads only the

@@ -55,6 +55,7 @@ SIGNATURES = {
     "blpg_options_init": (None, [C.POINTER(Options)]),
     "blpg_solve_batch": (C.c_int32, [C.POINTER(Batch), C.POINTER(Options), C.POINTER(Result)]),
     "blpg_solve_batch_chunks": (C.c_int32, []),
+    "blpg_release_workspace": (C.c_int32, []),
     "blpg_plan_create": (C.c_int32, [C.POINTER(Batch), C.POINTER(Options), C.POINTER(C.c_void_p)]),
     "blpg_plan_execute": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.POINTER(Result), C.c_void_p]),

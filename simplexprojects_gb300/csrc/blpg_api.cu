@@ -1413,6 +1413,38 @@ static int32_t solve_chunked(const blpg_batch* bt, const blpg_options& opt, blpg
 
 extern "C" int32_t blpg_solve_batch_chunks(void) { return blpg::g_last_chunks.load(); }
 
+extern "C" int32_t blpg_release_workspace(void) {
+  using namespace blpg;
+  {
+    std::lock_guard<std::mutex> lk(g_ws.mu);
+    if (g_ws.plan) blpg_plan_destroy(g_ws.plan);  // synchronises its stream
+    g_ws.plan = nullptr;
+    if (g_ws.buf) cudaFree(g_ws.buf);
+    g_ws.buf = nullptr;
+    g_ws.cap = 0;
+    g_ws.key_shapes.clear();
+    g_ws.key_negs.clear();
+    g_ws.key_offs.clear();
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_chunks.mu);
+    ChunkCache& cc = g_chunks;
+    if (cc.up) cudaStreamSynchronize(cc.up);
+    cc.clear();  // destroys the chunk plans (each synchronises its stream)
+    if (cc.up) cudaStreamDestroy(cc.up);
+    cc.up = nullptr;
+    if (cc.buf) cudaFree(cc.buf);
+    cc.buf = nullptr;
+    cc.cap = 0;
+    cc.ring = -1;
+    cc.bounds.clear();
+    cc.key_shapes.clear();
+    cc.key_negs.clear();
+    cc.key_offs.clear();
+  }
+  return BLPG_OK;
+}
+
 extern "C" int32_t blpg_solve_batch(const blpg_batch* bt, const blpg_options* opt_in,
                                     blpg_result* out) {
   if (!bt || !out || !out->status || !out->objective)

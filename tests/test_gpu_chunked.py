@@ -106,3 +106,25 @@ def test_chunked_solve_with_offsets(built, knobs, chunks):
     assert np.array_equal(f.status, cpu.status)
     rel = np.abs(f.objective - cpu.objective) / np.maximum(np.abs(cpu.objective), 1.0)
     assert rel[opt].max() <= 1e-6
+
+
+def test_release_workspace(built):
+    """blpg_release_workspace frees the cached plans and device buffers of
+    blpg_solve_batch (one-plan and chunked); the next call rebuilds them and
+    gives the same results."""
+    import torch
+    big = sp.generate(1, 3000, seed=sp.DEFAULT_SEED)     # chunked
+    small = sp.generate(0, 200, seed=sp.DEFAULT_SEED)    # one plan
+    a = sp.solve(big, "fp64", want_x=True)
+    s1 = sp.solve(small, "fp64")
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    N.check(N.lib().blpg_release_workspace(), "blpg_release_workspace")
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 - free0 >= 150 << 20  # at least the chunked batch's 183 MB device copy
+    b = sp.solve(big, "fp64", want_x=True)
+    s2 = sp.solve(small, "fp64")
+    assert np.array_equal(a.objective.view(np.uint64), b.objective.view(np.uint64))
+    assert np.array_equal(a.x.view(np.uint64), b.x.view(np.uint64))
+    assert np.array_equal(s1.objective.view(np.uint64), s2.objective.view(np.uint64))
+    N.check(N.lib().blpg_release_workspace(), "blpg_release_workspace")
