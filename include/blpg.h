@@ -427,6 +427,24 @@ int32_t blpg_read_abc(const char* path_A, const char* path_B,
                       const char* path_C, int32_t* m, int32_t* n, double* A,
                       double* b, double* c);
 
+/* Batch files: a whole batch (shapes, offsets, A, b, c) in one binary file
+ * ("BLPGBAT1", little-endian: magic, version, counts, m[], n[], off_A[],
+ * off_b[], off_c[], A, b, c; offsets always stored, so LPs that share A keep
+ * sharing it).  blpg_read_batch: call once with null arrays to get count
+ * and the stored element counts of A, b, c, then with buffers of those
+ * sizes (m, n: count int32; offsets: count int64).  blpg_write_results
+ * writes one line per LP, "status objective" and, when res->x is set, the
+ * LP's n values of x, all doubles as %.17g (exact round trip); path "-" is
+ * standard output.  No reference counterpart (the reference reads one LP's
+ * A/B/C files and replicates it). */
+int32_t blpg_write_batch(const char* path, const blpg_batch* batch);
+int32_t blpg_read_batch(const char* path, int64_t* count, int64_t* nA,
+                        int64_t* nb, int64_t* nc, int32_t* m, int32_t* n,
+                        int64_t* off_A, int64_t* off_b, int64_t* off_c,
+                        double* A, double* b, double* c);
+int32_t blpg_write_results(const char* path, const blpg_batch* batch,
+                           const blpg_result* res);
+
 /* Synthetic workloads.  kind 0..4:
  *  0  m=28, n=32, density 0.6
  *  1  m in {50,56,74,105}, n uniform on [m, 1.8m], density 0.6,

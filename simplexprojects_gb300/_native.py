@@ -99,6 +99,12 @@ SIGNATURES = {
     "blpg_topm_hint": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                    C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "blpg_read_abc": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, i32p, i32p, f64p, f64p, f64p]),
+    "blpg_write_batch": (C.c_int32, [C.c_char_p, C.POINTER(Batch)]),
+    "blpg_read_batch": (C.c_int32, [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                    C.POINTER(C.c_int64), C.POINTER(C.c_int64), i32p, i32p,
+                                    C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                    C.POINTER(C.c_int64), f64p, f64p, f64p]),
+    "blpg_write_results": (C.c_int32, [C.c_char_p, C.POINTER(Batch), C.POINTER(Result)]),
     "blpg_gen_shapes": (C.c_int64, [C.c_int32, C.c_int64, C.c_int32, C.c_uint64, i32p, i32p, i32p]),
     "blpg_gen_fill": (C.c_int32, [C.c_int32, C.c_int64, C.c_int32, C.c_uint64, i32p, i32p, f64p,
                                   f64p, f64p, C.c_int32]),

@@ -1,6 +1,7 @@
 // blpg_cli — the reference's command line over libblpg.
 //
 //   blpg_cli <benchmark-no | dimension> <average> <batch-size> <streams> <1|2>
+//   blpg_cli <batch-file> <average> <results-file | -> <64|32> 3
 //
 // Mirrors BLPGSolver (GPU_Tester.cu:31-393, ReadMe:10-20):
 //   mode 1: Netlib benchmark 1..8 (parseBenchmark.cpp:29-57) read from
@@ -11,6 +12,9 @@
 //           b_i ~ U{1..999}, c_j ~ U{1..499} as parseBenchmark.cpp:321-376
 //           (seeded here, so runs repeat; the reference only prints GLPK's
 //           answer in this mode and exits, GPU_Tester.cu:67-79).
+//   mode 3: a batch file (blpg_write_batch) solved as it stands, in FP64 or
+//           FP32, with the per-LP results written by blpg_write_results
+//           (status, objective, x; "-" writes them to stdout).
 // The batch is solved `average`+1 times; the first run is warm-up and the
 // rest are averaged (GPU_Tester.cu:242-262).  Batches larger than what fits
 // the device's free memory are split by the library (GPU_Tester.cu:194-238).
@@ -29,15 +33,62 @@ const char* kNames[8] = {"ADLITTLE", "AFIRO", "BLEND", "ISRAEL", "SC105", "SC205
 int usage() {
   std::printf(
       "usage: blpg_cli <benchmark-no|dimension> <average> <batch-size> <streams> <1|2>\n"
+      "       blpg_cli <batch-file> <average> <results-file|-> <64|32> 3\n"
       "  1: Netlib benchmark 1..8 from $BLPG_BENCH_DIR (default ./benchmarks)\n"
-      "  2: random dense LP of the given dimension\n");
+      "  2: random dense LP of the given dimension\n"
+      "  3: a batch file, results to a file (or stdout)\n");
   return 2;
+}
+
+int fail_with_last_error() {
+  std::fprintf(stderr, "%s\n", blpg_last_error());
+  return 1;
+}
+
+// mode 3: blpg_read_batch -> blpg_solve_batch (timed) -> blpg_write_results
+int solve_batch_file(const char* in, int avg, const char* out, int bits) {
+  int64_t count = 0, nA = 0, nb = 0, nc = 0;
+  if (blpg_read_batch(in, &count, &nA, &nb, &nc, nullptr, nullptr, nullptr, nullptr, nullptr,
+                      nullptr, nullptr, nullptr))
+    return fail_with_last_error();
+  std::vector<int32_t> m(count), n(count);
+  std::vector<int64_t> oA(count), ob(count), oc(count);
+  std::vector<double> A(nA), b(nb), c(nc);
+  if (blpg_read_batch(in, &count, &nA, &nb, &nc, m.data(), n.data(), oA.data(), ob.data(),
+                      oc.data(), A.data(), b.data(), c.data()))
+    return fail_with_last_error();
+  const blpg_batch bt{(int32_t)count, m.data(), n.data(), oA.data(), ob.data(), oc.data(),
+                      A.data(), b.data(), c.data()};
+  blpg_options opt;
+  blpg_options_init(&opt);
+  opt.precision = bits == 32 ? BLPG_FP32 : BLPG_FP64;
+  std::vector<int32_t> status(count), pivots(count);
+  std::vector<double> obj(count), x(nc);
+  blpg_result res{status.data(), obj.data(), x.data(), pivots.data(), nullptr, nullptr};
+  double sum = 0.0;
+  for (int it = 0; it <= avg; ++it) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (blpg_solve_batch(&bt, &opt, &res)) return fail_with_last_error();
+    const double sec =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::fprintf(stderr, "Iter %d: Time = %.6f Seconds\n", it, sec);
+    if (it > 0) sum += sec;
+  }
+  std::fprintf(stderr, "%lld LPs (FP%d): %.6f s, %.1f LPs/s\n", (long long)count, bits,
+               sum / avg, count / (sum / avg));
+  if (blpg_write_results(out, &bt, &res)) return fail_with_last_error();
+  return 0;
 }
 
 }  // namespace
 
 int main(int argc, char** argv) {
   if (argc != 6) return usage();
+  if (std::atoi(argv[5]) == 3) {
+    const int bits = std::atoi(argv[4]);
+    if (bits != 32 && bits != 64) return usage();
+    return solve_batch_file(argv[1], std::max(1, std::atoi(argv[2])), argv[3], bits);
+  }
   const int which = std::atoi(argv[1]);
   const int avg = std::max(1, std::atoi(argv[2]));
   const int batch = std::max(1, std::atoi(argv[3]));

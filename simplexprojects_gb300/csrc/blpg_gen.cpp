@@ -7,7 +7,9 @@
 // every LP is max c^T x, A x <= b, x >= 0 with b >= 0, so the origin is
 // feasible and the slack basis is a valid start, as in the reference's
 // single-phase path (simplex.cu:874-890).
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -304,5 +306,149 @@ extern "C" int32_t blpg_read_abc(const char* path_A, const char* path_B,
   for (long e = 0; e < rows * cols; ++e) A[e] = av[e] == 0.0 ? 0.0 : av[e];
   for (long i = 0; i < rows; ++i) b[i] = bv[i];
   for (long j = 0; j < cols; ++j) c[j] = cv[j];
+  return BLPG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batch files: a whole batch (shapes, offsets, A, b, c) in one binary file,
+// and the per-LP results as text, one line per LP.  No reference
+// counterpart: the reference only reads one LP's A/B/C text files
+// (parseBenchmark.cpp:59-126) and replicates it (GPU_Tester.cu:119-127).
+//
+// Layout (little-endian, the byte order of the hosts this library runs on):
+//   char    magic[8] = "BLPGBAT1"
+//   uint32  version = 1, uint32 reserved = 0
+//   int64   count, nA, nb, nc      (elements of A, b, c stored)
+//   int32   m[count], n[count]
+//   int64   off_A[count], off_b[count], off_c[count]
+//   double  A[nA], b[nb], c[nc]
+// Offsets are always stored (packed ones when the batch had none), so LPs
+// that share A keep sharing it in the file.
+// ---------------------------------------------------------------------------
+namespace {
+
+const char kBatchMagic[8] = {'B', 'L', 'P', 'G', 'B', 'A', 'T', '1'};
+
+struct FileCloser {
+  std::FILE* f;
+  ~FileCloser() {
+    if (f) std::fclose(f);
+  }
+};
+
+bool little_endian() {
+  const uint32_t one = 1;
+  unsigned char c0;
+  std::memcpy(&c0, &one, 1);
+  return c0 == 1;
+}
+
+}  // namespace
+
+extern "C" int32_t blpg_write_batch(const char* path, const blpg_batch* bt) {
+  using blpg::fail;
+  if (!path || !bt || bt->count < 0 || (bt->count > 0 && (!bt->m || !bt->n || !bt->A || !bt->b || !bt->c)))
+    return fail(BLPG_EINVAL, "blpg_write_batch: null or negative argument");
+  if (!little_endian()) return fail(BLPG_EIO, "blpg_write_batch: big-endian host");
+  const int64_t N = bt->count;
+  std::vector<int64_t> oA(N), ob(N), oc(N);
+  int64_t pa = 0, pb = 0, pc = 0, nA = 0, nb = 0, nc = 0;
+  for (int64_t k = 0; k < N; ++k) {
+    const int64_t m = bt->m[k], n = bt->n[k];
+    if (m < 0 || n < 0) return fail(BLPG_EINVAL, "blpg_write_batch: LP %lld has a negative size", (long long)k);
+    oA[k] = bt->off_A ? bt->off_A[k] : pa;
+    ob[k] = bt->off_b ? bt->off_b[k] : pb;
+    oc[k] = bt->off_c ? bt->off_c[k] : pc;
+    if (oA[k] < 0 || ob[k] < 0 || oc[k] < 0)
+      return fail(BLPG_EINVAL, "blpg_write_batch: LP %lld has a negative offset", (long long)k);
+    pa += m * n;
+    pb += m;
+    pc += n;
+    nA = std::max(nA, oA[k] + m * n);
+    nb = std::max(nb, ob[k] + m);
+    nc = std::max(nc, oc[k] + n);
+  }
+  std::FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(BLPG_EIO, "blpg_write_batch: cannot create %s", path);
+  FileCloser fc{f};
+  const uint32_t ver[2] = {1u, 0u};
+  const int64_t sizes[4] = {N, nA, nb, nc};
+  bool ok = std::fwrite(kBatchMagic, 1, 8, f) == 8 && std::fwrite(ver, 4, 2, f) == 2 &&
+            std::fwrite(sizes, 8, 4, f) == 4;
+  ok = ok && std::fwrite(bt->m, 4, (size_t)N, f) == (size_t)N &&
+       std::fwrite(bt->n, 4, (size_t)N, f) == (size_t)N;
+  ok = ok && std::fwrite(oA.data(), 8, (size_t)N, f) == (size_t)N &&
+       std::fwrite(ob.data(), 8, (size_t)N, f) == (size_t)N &&
+       std::fwrite(oc.data(), 8, (size_t)N, f) == (size_t)N;
+  ok = ok && std::fwrite(bt->A, 8, (size_t)nA, f) == (size_t)nA &&
+       std::fwrite(bt->b, 8, (size_t)nb, f) == (size_t)nb &&
+       std::fwrite(bt->c, 8, (size_t)nc, f) == (size_t)nc;
+  if (!ok) return fail(BLPG_EIO, "blpg_write_batch: write to %s failed", path);
+  return BLPG_OK;
+}
+
+extern "C" int32_t blpg_read_batch(const char* path, int64_t* count, int64_t* nA, int64_t* nb,
+                                   int64_t* nc, int32_t* m, int32_t* n, int64_t* off_A,
+                                   int64_t* off_b, int64_t* off_c, double* A, double* b,
+                                   double* c) {
+  using blpg::fail;
+  if (!path || !count || !nA || !nb || !nc) return fail(BLPG_EINVAL, "blpg_read_batch: null argument");
+  if (!little_endian()) return fail(BLPG_EIO, "blpg_read_batch: big-endian host");
+  std::FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(BLPG_EIO, "blpg_read_batch: cannot open %s", path);
+  FileCloser fc{f};
+  char magic[8];
+  uint32_t ver[2];
+  int64_t sizes[4];
+  if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kBatchMagic, 8) != 0)
+    return fail(BLPG_EIO, "blpg_read_batch: %s is not a batch file", path);
+  if (std::fread(ver, 4, 2, f) != 2 || ver[0] != 1u)
+    return fail(BLPG_EIO, "blpg_read_batch: %s: unsupported version", path);
+  if (std::fread(sizes, 8, 4, f) != 4 || sizes[0] < 0 || sizes[0] > INT32_MAX || sizes[1] < 0 ||
+      sizes[2] < 0 || sizes[3] < 0)
+    return fail(BLPG_EIO, "blpg_read_batch: %s: bad header", path);
+  *count = sizes[0];
+  *nA = sizes[1];
+  *nb = sizes[2];
+  *nc = sizes[3];
+  const bool none = !m && !n && !off_A && !off_b && !off_c && !A && !b && !c;
+  if (none) return BLPG_OK;
+  if (!m || !n || !off_A || !off_b || !off_c || !A || !b || !c)
+    return fail(BLPG_EINVAL, "blpg_read_batch: partial buffers");
+  const size_t N = (size_t)sizes[0];
+  bool ok = std::fread(m, 4, N, f) == N && std::fread(n, 4, N, f) == N &&
+            std::fread(off_A, 8, N, f) == N && std::fread(off_b, 8, N, f) == N &&
+            std::fread(off_c, 8, N, f) == N;
+  ok = ok && std::fread(A, 8, (size_t)sizes[1], f) == (size_t)sizes[1] &&
+       std::fread(b, 8, (size_t)sizes[2], f) == (size_t)sizes[2] &&
+       std::fread(c, 8, (size_t)sizes[3], f) == (size_t)sizes[3];
+  if (!ok) return fail(BLPG_EIO, "blpg_read_batch: %s is truncated", path);
+  for (size_t k = 0; k < N; ++k) {
+    const int64_t mk = m[k], nk = n[k];
+    if (mk < 0 || nk < 0 || off_A[k] < 0 || off_b[k] < 0 || off_c[k] < 0 ||
+        off_A[k] + mk * nk > sizes[1] || off_b[k] + mk > sizes[2] || off_c[k] + nk > sizes[3])
+      return fail(BLPG_EIO, "blpg_read_batch: %s: LP %zu lies outside the stored arrays", path, k);
+  }
+  return BLPG_OK;
+}
+
+extern "C" int32_t blpg_write_results(const char* path, const blpg_batch* bt,
+                                      const blpg_result* res) {
+  using blpg::fail;
+  if (!path || !bt || !res || (bt->count > 0 && (!bt->n || !res->status || !res->objective)))
+    return fail(BLPG_EINVAL, "blpg_write_results: null argument");
+  std::FILE* f = std::strcmp(path, "-") == 0 ? stdout : std::fopen(path, "w");
+  if (!f) return fail(BLPG_EIO, "blpg_write_results: cannot create %s", path);
+  FileCloser fc{f == stdout ? nullptr : f};
+  int64_t pc = 0;
+  for (int64_t k = 0; k < bt->count; ++k) {
+    const int64_t oc = bt->off_c ? bt->off_c[k] : pc;
+    pc += bt->n[k];
+    std::fprintf(f, "%d %.17g", res->status[k], res->objective[k]);
+    if (res->x)
+      for (int32_t j = 0; j < bt->n[k]; ++j) std::fprintf(f, " %.17g", res->x[oc + j]);
+    std::fputc('\n', f);
+  }
+  if (std::ferror(f)) return fail(BLPG_EIO, "blpg_write_results: write to %s failed", path);
   return BLPG_OK;
 }

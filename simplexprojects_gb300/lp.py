@@ -244,3 +244,44 @@ def read_abc(path_A: str, path_B: str, path_C: str):
                             C.byref(n), N.ptr(A, C.c_double), N.ptr(b, C.c_double),
                             N.ptr(c, C.c_double)), "blpg_read_abc")
     return A.reshape(m.value, n.value), b, c
+
+
+def write_batch(path: str, batch: LPBatch) -> None:
+    """A batch in one binary file (blpg_write_batch: shapes, offsets, A, b, c;
+    LPs that share A keep sharing it)."""
+    bst = batch.c_struct()
+    N.check(N.lib().blpg_write_batch(str(path).encode(), C.byref(bst)), "blpg_write_batch")
+
+
+def read_batch(path: str) -> LPBatch:
+    """The batch a batch file holds (blpg_read_batch), offsets included."""
+    L = N.lib()
+    cnt, na, nb, nc = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+    p = str(path).encode()
+    N.check(L.blpg_read_batch(p, C.byref(cnt), C.byref(na), C.byref(nb), C.byref(nc), None, None,
+                              None, None, None, None, None, None), "blpg_read_batch")
+    k = cnt.value
+    m, n = np.empty(k, np.int32), np.empty(k, np.int32)
+    oA, ob, oc = np.empty(k, np.int64), np.empty(k, np.int64), np.empty(k, np.int64)
+    A, b, c = np.empty(na.value), np.empty(nb.value), np.empty(nc.value)
+    if k == 0:
+        return LPBatch(m, n, A, b, c, off_A=oA, off_b=ob, off_c=oc)
+    N.check(L.blpg_read_batch(p, C.byref(cnt), C.byref(na), C.byref(nb), C.byref(nc),
+                              N.ptr(m, C.c_int32), N.ptr(n, C.c_int32), N.ptr(oA, C.c_int64),
+                              N.ptr(ob, C.c_int64), N.ptr(oc, C.c_int64), N.ptr(A, C.c_double),
+                              N.ptr(b, C.c_double), N.ptr(c, C.c_double)), "blpg_read_batch")
+    return LPBatch(m, n, A, b, c, off_A=oA, off_b=ob, off_c=oc)
+
+
+def write_results(path: str, batch: LPBatch, status, objective, x=None) -> None:
+    """One text line per LP (blpg_write_results): the status, the objective
+    and, when x is given, x in the batch's c layout, every double printed with
+    17 significant digits so it reads back bit for bit. path "-" is stdout."""
+    st = np.ascontiguousarray(status, dtype=np.int32)
+    ob = np.ascontiguousarray(objective, dtype=np.float64)
+    xs = None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+    res = N.Result(N.ptr(st, C.c_int32), N.ptr(ob, C.c_double),
+                   None if xs is None else N.ptr(xs, C.c_double), None, None, None)
+    bst = batch.c_struct()
+    N.check(N.lib().blpg_write_results(str(path).encode(), C.byref(bst), C.byref(res)),
+            "blpg_write_results")
