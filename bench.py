@@ -365,7 +365,9 @@ def run_learned(args, rank, world, local, dist=None):
         "status_match": float((res.status == pres.status).mean()),
         "max_rel_obj_err_vs_fp64": float(rel.max()) if rel.size else 0.0,
         "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "LPs/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": int(total * 16), "ms_per_step": e2e_ms,
+                # status, pivots, info (4 bytes each) and the objective (8)
+                "d2h_bytes_per_step": int(total * 20), "ms_per_step": e2e_ms,
+                "step_ms_all": [round(t * 1e3, 3) for t in e2e],
                 "call": "blpg_learned_solve (include/blpg.h)"},
         "roofline": {"bound": "smem", "achieved": ach, "peak": smem.value, "unit": "GB/s",
                      "frac": ach / smem.value, "traffic": KIND3_SOLVE_DRAM_BYTES,

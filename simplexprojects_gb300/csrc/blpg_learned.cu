@@ -7,10 +7,13 @@
 // otherwise chain by hand (blpg_features, blpg_mlp_predict,
 // blpg_price_weights, blpg_plan_execute_weighted).
 //
-// Everything is enqueued on one stream in that order, except A's upload,
-// which runs on a second stream beside the network and which the solve
-// waits for; host arrays in pinned memory make the uploads and downloads
-// asynchronous to the host until the final synchronisation.
+// The uploads run on a copy stream in three pieces, b/c/family ids of the
+// first half of the LPs, then of the second half, then A; the network of
+// each half runs on the compute stream as soon as its piece has landed, so
+// the second half's upload and A's overlap the first half's network, and
+// the solve waits for A.  The results come back in one copy of a packed
+// device block into pinned staging, then into the caller's arrays.  Host
+// input arrays in pinned memory make the uploads asynchronous to the host.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,13 +29,21 @@ struct blpg_learned {
   float beta = 1.f;
   int d_in_pad = 0, d_out_pad = 0, rows = 0;
   int64_t extA = 0, extb = 0, extc = 0, extw = 0;
+  // the LPs [0, half) form the first upload and network piece (half a
+  // multiple of 64, so each piece's network rows are); its b and c lie in
+  // [0, eb1) and [0, ec1); half == count: one piece
+  int half = 0;
+  int64_t eb1 = 0, ec1 = 0;
   cudaStream_t stream = nullptr;
-  cudaStream_t stream_a = nullptr;  // A's upload, beside the network
-  cudaEvent_t a_landed = nullptr;
-  // device buffers
+  cudaStream_t stream_a = nullptr;  // uploads, beside the network
+  cudaEvent_t first_landed = nullptr, all_landed = nullptr, a_landed = nullptr;
+  // device buffers; obj, st, piv, info are one block (res) so that the
+  // results download in one copy, into pinned staging (hres)
   double *A = nullptr, *b = nullptr, *c = nullptr, *obj = nullptr, *x = nullptr;
   int32_t *fam = nullptr, *dm = nullptr, *dn = nullptr, *st = nullptr, *piv = nullptr,
           *info = nullptr;
+  void* res = nullptr;
+  unsigned char* hres = nullptr;
   int64_t *offb = nullptr, *offc = nullptr, *offw = nullptr;
   float *mean = nullptr, *std_ = nullptr, *X = nullptr, *logits = nullptr, *w = nullptr;
 };
@@ -47,13 +58,18 @@ namespace {
                         "blpg_learned: %s: %s", #call, cudaGetErrorString(e_));             \
   } while (0)
 
+// objective (8 bytes), status, pivots and info (4 each) per LP
+constexpr size_t kResBytesPerLp = 20;
+
 void release(blpg_learned* L) {
   if (!L) return;
   if (L->plan) blpg_plan_destroy(L->plan);
-  void* bufs[] = {L->A, L->b, L->c, L->obj, L->x, L->fam, L->dm, L->dn, L->st, L->piv, L->info,
-                  L->offb, L->offc, L->offw, L->mean, L->std_, L->X, L->logits, L->w};
+  void* bufs[] = {L->A,    L->b,    L->c,    L->x,    L->fam,   L->dm, L->dn,     L->res,
+                  L->offb, L->offc, L->offw, L->mean, L->std_, L->X,  L->logits, L->w};
   for (void* p : bufs) cudaFree(p);
-  if (L->a_landed) cudaEventDestroy(L->a_landed);
+  if (L->hres) cudaFreeHost(L->hres);
+  for (cudaEvent_t ev : {L->first_landed, L->all_landed, L->a_landed})
+    if (ev) cudaEventDestroy(ev);
   if (L->stream_a) cudaStreamDestroy(L->stream_a);
   if (L->stream) cudaStreamDestroy(L->stream);
 }
@@ -122,9 +138,17 @@ extern "C" int32_t blpg_learned_create(blpg_mlp* mlp, int32_t families, const fl
     pc += n;
   }
   L->extw = (int64_t)N * (n + m);
+  // two pieces from 512 LPs up (below that the second network launch costs
+  // more than the upload it hides)
+  L->half = N >= 512 ? (N / 2 + 63) / 64 * 64 : N;
+  for (int k = 0; k < L->half; ++k) {
+    L->eb1 = std::max(L->eb1, ob[k] + m);
+    L->ec1 = std::max(L->ec1, oc[k] + n);
+  }
   cudaError_t e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L->stream_a, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L->a_landed, cudaEventDisableTiming);
+  for (cudaEvent_t* ev : {&L->first_landed, &L->all_landed, &L->a_landed})
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
   if (e != cudaSuccess) return bail(fail(BLPG_ECUDA, "blpg_learned_create: stream"));
   const size_t F = (size_t)families * (n + m);
 #define LMAL(p, bytes)                                                              \
@@ -135,14 +159,18 @@ extern "C" int32_t blpg_learned_create(blpg_mlp* mlp, int32_t families, const fl
   LMAL(L->A, sizeof(double) * (size_t)L->extA);
   LMAL(L->b, sizeof(double) * (size_t)L->extb);
   LMAL(L->c, sizeof(double) * (size_t)L->extc);
-  LMAL(L->obj, sizeof(double) * N);
+  LMAL(L->res, kResBytesPerLp * (size_t)N);
+  if (cudaMallocHost(&L->hres, kResBytesPerLp * (size_t)N) != cudaSuccess)
+    return bail(fail(BLPG_ENOMEM, "blpg_learned_create: %zu pinned bytes",
+                     kResBytesPerLp * (size_t)N));
+  L->obj = static_cast<double*>(L->res);  // [0, 8N) objectives
+  L->st = reinterpret_cast<int32_t*>(L->obj + N);  // [8N, 12N) statuses
+  L->piv = L->st + N;                              // [12N, 16N) pivots
+  L->info = L->piv + N;                            // [16N, 20N) info bits
   LMAL(L->x, sizeof(double) * (size_t)L->extc);
   LMAL(L->fam, sizeof(int32_t) * N);
   LMAL(L->dm, sizeof(int32_t) * N);
   LMAL(L->dn, sizeof(int32_t) * N);
-  LMAL(L->st, sizeof(int32_t) * N);
-  LMAL(L->piv, sizeof(int32_t) * N);
-  LMAL(L->info, sizeof(int32_t) * N);
   LMAL(L->offb, sizeof(int64_t) * N);
   LMAL(L->offc, sizeof(int64_t) * N);
   LMAL(L->offw, sizeof(int64_t) * N);
@@ -176,21 +204,44 @@ extern "C" int32_t blpg_learned_solve(blpg_learned* L, const blpg_batch* bt,
     return fail(BLPG_EINVAL, "blpg_learned_solve: null argument");
   if (bt->count != L->count || !bt->A || !bt->b || !bt->c)
     return fail(BLPG_EINVAL, "blpg_learned_solve: the batch is not the one the solver was made for");
-  const int N = L->count;
-  cudaStream_t s = L->stream;
-  // A is read only by the solve: its upload runs on a second stream while b,
-  // c and the family ids upload and the network runs
-  LCK(cudaMemcpyAsync(L->A, bt->A, sizeof(double) * (size_t)L->extA, cudaMemcpyHostToDevice,
-                      L->stream_a));
-  LCK(cudaEventRecord(L->a_landed, L->stream_a));
-  LCK(cudaMemcpyAsync(L->b, bt->b, sizeof(double) * (size_t)L->extb, cudaMemcpyHostToDevice, s));
-  LCK(cudaMemcpyAsync(L->c, bt->c, sizeof(double) * (size_t)L->extc, cudaMemcpyHostToDevice, s));
-  LCK(cudaMemcpyAsync(L->fam, host_family, sizeof(int32_t) * N, cudaMemcpyHostToDevice, s));
+  const int N = L->count, H = L->half;
+  cudaStream_t s = L->stream, u = L->stream_a;
+  const size_t d8 = sizeof(double);
+  // the first piece's b, c and family ids, then its features and network
+  LCK(cudaMemcpyAsync(L->b, bt->b, d8 * (size_t)L->eb1, cudaMemcpyHostToDevice, u));
+  LCK(cudaMemcpyAsync(L->c, bt->c, d8 * (size_t)L->ec1, cudaMemcpyHostToDevice, u));
+  LCK(cudaMemcpyAsync(L->fam, host_family, sizeof(int32_t) * H, cudaMemcpyHostToDevice, u));
+  LCK(cudaEventRecord(L->first_landed, u));
+  LCK(cudaStreamWaitEvent(s, L->first_landed, 0));
   int32_t rc;
-  if ((rc = blpg_features(N, L->m, L->n, L->families, L->offb, L->offc, L->b, L->c, L->fam,
+  if ((rc = blpg_features(H, L->m, L->n, L->families, L->offb, L->offc, L->b, L->c, L->fam,
                           L->mean, L->std_, L->X, L->d_in_pad, s)))
     return rc;
-  if ((rc = blpg_mlp_predict(L->mlp, L->X, L->rows, L->logits, s))) return rc;
+  const int rows1 = H < N ? H : L->rows;
+  if ((rc = blpg_mlp_predict(L->mlp, L->X, rows1, L->logits, s))) return rc;
+  // the rest: the second piece (what the first did not cover), its network
+  if (H < N) {
+    if (L->extb > L->eb1)
+      LCK(cudaMemcpyAsync(L->b + L->eb1, bt->b + L->eb1, d8 * (size_t)(L->extb - L->eb1),
+                          cudaMemcpyHostToDevice, u));
+    if (L->extc > L->ec1)
+      LCK(cudaMemcpyAsync(L->c + L->ec1, bt->c + L->ec1, d8 * (size_t)(L->extc - L->ec1),
+                          cudaMemcpyHostToDevice, u));
+    LCK(cudaMemcpyAsync(L->fam + H, host_family + H, sizeof(int32_t) * (N - H),
+                        cudaMemcpyHostToDevice, u));
+    LCK(cudaEventRecord(L->all_landed, u));
+    LCK(cudaStreamWaitEvent(s, L->all_landed, 0));
+    if ((rc = blpg_features(N - H, L->m, L->n, L->families, L->offb + H, L->offc + H, L->b, L->c,
+                            L->fam + H, L->mean, L->std_, L->X + (size_t)H * L->d_in_pad,
+                            L->d_in_pad, s)))
+      return rc;
+    if ((rc = blpg_mlp_predict(L->mlp, L->X + (size_t)H * L->d_in_pad, L->rows - H,
+                               L->logits + (size_t)H * L->d_out_pad, s)))
+      return rc;
+  }
+  // A last: only the solve reads it
+  LCK(cudaMemcpyAsync(L->A, bt->A, d8 * (size_t)L->extA, cudaMemcpyHostToDevice, u));
+  LCK(cudaEventRecord(L->a_landed, u));
   if ((rc = blpg_price_weights(L->logits, L->d_out_pad, N, L->dm, L->dn, L->n + L->m, L->offw,
                                L->beta, L->w, s)))
     return rc;
@@ -199,16 +250,18 @@ extern "C" int32_t blpg_learned_solve(blpg_learned* L, const blpg_batch* bt,
   LCK(cudaStreamWaitEvent(s, L->a_landed, 0));
   if ((rc = blpg_plan_execute_weighted(L->plan, L->A, L->b, L->c, nullptr, L->w, &dres, s)))
     return rc;
-  LCK(cudaMemcpyAsync(out->status, L->st, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, s));
-  LCK(cudaMemcpyAsync(out->objective, L->obj, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+  // one download of the packed results (objectives and statuses, then the
+  // pivots and info bits when asked for)
+  const size_t nres = (size_t)N * (out->info ? 20 : out->pivots ? 16 : 12);
+  LCK(cudaMemcpyAsync(L->hres, L->res, nres, cudaMemcpyDeviceToHost, s));
   if (out->x)
-    LCK(cudaMemcpyAsync(out->x, L->x, sizeof(double) * (size_t)L->extc, cudaMemcpyDeviceToHost,
-                        s));
-  if (out->pivots)
-    LCK(cudaMemcpyAsync(out->pivots, L->piv, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, s));
-  if (out->info)
-    LCK(cudaMemcpyAsync(out->info, L->info, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, s));
+    LCK(cudaMemcpyAsync(out->x, L->x, d8 * (size_t)L->extc, cudaMemcpyDeviceToHost, s));
   LCK(cudaStreamSynchronize(s));
+  const unsigned char* h = L->hres;
+  std::memcpy(out->objective, h, d8 * N);
+  std::memcpy(out->status, h + 8 * (size_t)N, sizeof(int32_t) * N);
+  if (out->pivots) std::memcpy(out->pivots, h + 12 * (size_t)N, sizeof(int32_t) * N);
+  if (out->info) std::memcpy(out->info, h + 16 * (size_t)N, sizeof(int32_t) * N);
   return BLPG_OK;
 }
 

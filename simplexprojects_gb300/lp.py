@@ -52,13 +52,15 @@ class LPBatch:
 
     def offsets(self):
         """(off_A, off_b, off_c), computing packed offsets where absent."""
-        mn = self.m.astype(np.int64) * self.n
-        pa = np.concatenate([[0], np.cumsum(mn)[:-1]]).astype(np.int64)
-        pb = np.concatenate([[0], np.cumsum(self.m.astype(np.int64))[:-1]]).astype(np.int64)
-        pc = np.concatenate([[0], np.cumsum(self.n.astype(np.int64))[:-1]]).astype(np.int64)
-        return (self.off_A if self.off_A is not None else pa,
-                self.off_b if self.off_b is not None else pb,
-                self.off_c if self.off_c is not None else pc)
+        def packed(sizes):
+            out = np.zeros(sizes.size, np.int64)
+            np.cumsum(sizes[:-1], out=out[1:])
+            return out
+
+        return (self.off_A if self.off_A is not None else
+                packed(self.m.astype(np.int64) * self.n),
+                self.off_b if self.off_b is not None else packed(self.m.astype(np.int64)),
+                self.off_c if self.off_c is not None else packed(self.n.astype(np.int64)))
 
     def lp(self, k: int):
         """(A_k as an m x n array, b_k, c_k) for LP k."""
@@ -90,12 +92,28 @@ class LPBatch:
                        np.concatenate(cs) if cs else np.zeros(0), family=fam,
                        meta=dict(self.meta, subset=True))
 
+    def __getstate__(self):
+        """Pickled and deep-copied without the cached ctypes view."""
+        state = dict(self.__dict__)
+        state.pop("_c_struct", None)
+        return state
+
     def c_struct(self) -> N.Batch:
-        """ctypes view; the arrays must outlive the returned struct."""
-        return N.Batch(self.count, N.ptr(self.m, C.c_int32), N.ptr(self.n, C.c_int32),
-                       N.ptr(self.off_A, C.c_int64), N.ptr(self.off_b, C.c_int64),
-                       N.ptr(self.off_c, C.c_int64), N.ptr(self.A, C.c_double),
-                       N.ptr(self.b, C.c_double), N.ptr(self.c, C.c_double))
+        """ctypes view; the arrays must outlive the returned struct.  The view
+        is kept with references to the arrays it points into and reused while
+        the same array objects are in place (the references keep them alive,
+        so a reused view never points at freed memory); each call returns its
+        own copy of it, which the caller may change."""
+        arrays = (self.m, self.n, self.off_A, self.off_b, self.off_c, self.A, self.b, self.c)
+        cached = self.__dict__.get("_c_struct")
+        if cached is not None and all(x is y for x, y in zip(cached[0], arrays)):
+            return N.Batch.from_buffer_copy(cached[1])
+        bst = N.Batch(self.count, N.ptr(self.m, C.c_int32), N.ptr(self.n, C.c_int32),
+                      N.ptr(self.off_A, C.c_int64), N.ptr(self.off_b, C.c_int64),
+                      N.ptr(self.off_c, C.c_int64), N.ptr(self.A, C.c_double),
+                      N.ptr(self.b, C.c_double), N.ptr(self.c, C.c_double))
+        self.__dict__["_c_struct"] = (arrays, bst)
+        return N.Batch.from_buffer_copy(bst)
 
     def nbytes(self) -> int:
         return int(self.A.nbytes + self.b.nbytes + self.c.nbytes)

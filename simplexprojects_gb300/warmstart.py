@@ -399,8 +399,10 @@ class LearnedSolver:
             ob = np.zeros(k, np.float64)
             pv = np.zeros(k, np.int32)
             info = np.zeros(k, np.int32)
-            _, _, oc = batch.offsets()
-            x = np.zeros(int((oc + batch.n).max())) if want_x else None
+            x = None
+            if want_x:
+                _, _, oc = batch.offsets()
+                x = np.zeros(int((oc + batch.n).max()))
             res = N.Result(N.ptr(st, C.c_int32), N.ptr(ob, C.c_double), N.ptr(x, C.c_double),
                            N.ptr(pv, C.c_int32), None, N.ptr(info, C.c_int32))
             fam = np.ascontiguousarray(batch.family, dtype=np.int32)

@@ -64,3 +64,18 @@ def test_shared_batch_layout(built):
     bt = sp.LPBatch.shared(A, [1, 2], np.ones((4, 3)))
     assert bt.count == 4 and bt.off_A.tolist() == [0, 0, 0, 0]
     assert np.array_equal(bt.lp(3)[0], A)
+
+
+def test_batch_view_copies_are_independent(built):
+    """LPBatch.c_struct reuses one ctypes view while the arrays stay the same
+    objects, hands out copies (a caller nulling a field does not change the
+    next view) and rebuilds the view when an array is replaced."""
+    b = sp.generate(1, 20, seed=3)
+    first = b.c_struct()
+    first.A = None
+    first.c = None
+    again = b.c_struct()
+    assert C.addressof(again.A.contents) == b.A.ctypes.data
+    assert C.addressof(again.c.contents) == b.c.ctypes.data
+    b.c = b.c.copy()
+    assert C.addressof(b.c_struct().c.contents) == b.c.ctypes.data
