@@ -160,7 +160,7 @@ struct Geom {
 // nv, so a CTA lays out each LP it takes within its allocation and a class
 // only needs the largest member's total.
 struct Layout {
-  int tab, colA, colB, rhsx, basis, flags, cvar, vpos, ext, red, state, gam, total;
+  int tab, colA, colB, rhsx, basis, flags, cvar, vpos, ext, red, state, gam, gbytes, total;
   __host__ __device__ Layout(int m, int ldw, int nv, int elem, int se = 0) {
     const int mp1 = round_up(m + 1, 4);
     const int nvp = round_up(nv, 4);
@@ -193,13 +193,16 @@ struct Layout {
     // sharing the refresh's region when it is large enough (the norms are
     // recomputed after every refresh)
     gam = -1;
+    gbytes = 0;
     if (se) {
       if (ext_bytes >= ldw * 8) {
         gam = ext;
+        gbytes = ext_bytes;
       } else {
         off = round_up(off, 16);
         gam = off;
-        off += round_up(ldw * 8, 16);
+        gbytes = round_up(ldw * 8, 16);
+        off += gbytes;
       }
     }
     total = off;
@@ -470,6 +473,13 @@ __device__ __forceinline__ void norm_add(uint2* gcol, float v) {
 __device__ __forceinline__ float norm_gamma(uint2 gv) {
   return 1.f + ((float)gv.y + (float)gv.x * (1.f / 16777216.f));
 }
+// The FP32 single-CTA steepest-edge loop keeps the norms as partial sums
+// instead, when they fit the norm region: row group g of the sweep stores its
+// sums of squares of local slots [0, cw) in row g of a G x cw float array
+// (one 16-byte store per thread, no atomics), clamped like the counters, and
+// pricing adds the G partials of a column in group order, so the sum is the
+// same on every run.
+__device__ __forceinline__ float norm_clamp(float v) { return fminf(v, 33554432.f); }
 
 // Status codes (GLPK numbering, as blpg.h)
 constexpr int kUndef = 1, kNoFeas = 4, kOpt = 5, kUnbnd = 6;
@@ -513,6 +523,8 @@ struct Solver {
   int* cvar;   // slot -> variable id (every slot of the LP, replicated per CTA)
   int* vpos;   // variable -> slot if nonbasic, -1 - row if basic
   uint2* gam;  // steepest edge: fixed-point column norms of the local slots
+  float* npart;  // or their per-row-group partial sums (null: the counters)
+  int npitch, ngrp;  // partial sums: row pitch (cw) and row groups
   double* xr;  // FP64 x_B of the refresh (FP32 tableaux, FP64 ones with steepest edge)
   double* yr;  // FP64 duals of the refresh
   float* rf;   // the refresh's residuals rounded to FP32 / a 32-bit list
@@ -740,7 +752,7 @@ struct Solver {
   // The RHS replica is not extracted: the next ratio test reads the tableau.
   __device__ void update_body_se32(const Geom& g, int r, const T* fcol, int lc) {
     update_rows<true, true>(tab, rhsx, rank, g.m, g.ldw, g.nl, g.cw, r, -1, fcol, -1, -1, 0,
-                            nullptr, gam, lc);
+                            nullptr, gam, lc, npart);
   }
   // Kept out of line with plain arguments (no `this`, no structs by
   // reference) so that the unrolled sweep has its own register budget and
@@ -753,7 +765,8 @@ struct Solver {
                                                   const int cw, const int r, const int s,
                                                   const T* pcol, const int qn, const int owner_n,
                                                   const int c0, T* colx_next,
-                                                  uint2* gam, const int lc) {
+                                                  uint2* gam, const int lc,
+                                                  float* part = nullptr) {
     const int nt = (int)blockDim.x;
     const int G = SE ? min(nt / nl, kMaxNormGroups) : nt / nl;  // rows of lanes
     const int grp = threadIdx.x / nl;
@@ -816,13 +829,18 @@ struct Solver {
     for (; i0 < m; i0 += G)
       row(i0, pcol[i0], *reinterpret_cast<const VT*>(tb + (size_t)i0 * ldw + lane * V));
     if (SE) {
-      // columns visited in a rotated order, so that the counter pairs of one
-      // instruction fall in distinct banks (two wavefronts, not eight)
+      if (PRE && part) {
+        // this row group's partial sums of slots [0, cw), one store
+        if (lane * V < cw) store_partials(part + (size_t)grp * cw + lane * V, sq);
+      } else {
+        // columns visited in a rotated order, so that the counter pairs of one
+        // instruction fall in distinct banks (two wavefronts, not eight)
 #pragma unroll
-      for (int e2 = 0; e2 < V; ++e2) {
-        const int e = (e2 + (lane >> 2)) & (V - 1);
-        const int lj = lane * V + e;
-        if (lj < lc) norm_add(&gam[lj], sq_get(sq, e));
+        for (int e2 = 0; e2 < V; ++e2) {
+          const int e = (e2 + (lane >> 2)) & (V - 1);
+          const int lj = lane * V + e;
+          if (lj < lc) norm_add(&gam[lj], sq_get(sq, e));
+        }
       }
     }
     if (has_q && grp == 0) colx_next[m] = tb[(size_t)m * ldw + qloc];
@@ -904,7 +922,34 @@ struct Solver {
   // Column norms gamma_j = 1 + sum_{i<m} T_ij^2 of the current tableau,
   // recomputed with a full pass (at the start of a pricing loop, after
   // loads, crashes, refreshes and pivots made without norms).
+  // Partial sums of squares of one lane's V slots, clamped as the counters are.
+  static __device__ __forceinline__ void store_partials(float* dst, const float4& sq) {
+    *reinterpret_cast<float4*>(dst) = make_float4(norm_clamp(sq.x), norm_clamp(sq.y),
+                                                  norm_clamp(sq.z), norm_clamp(sq.w));
+  }
+  static __device__ __forceinline__ void store_partials(float* dst, const float2& sq) {
+    *reinterpret_cast<float2*>(dst) = make_float2(norm_clamp(sq.x), norm_clamp(sq.y));
+  }
+  // gamma_j of local slot lj from the partial sums, added in row-group order.
+  __device__ __forceinline__ float part_gamma(int lj) const {
+    float acc = 0.f;
+    for (int q = 0; q < ngrp; ++q) acc += npart[q * npitch + lj];
+    return 1.f + acc;
+  }
   __device__ void norms_full(const Geom& g, int lc) {
+    if (npart) {
+      // the partial sums of every row group, grouped as the sweep groups
+      // them; each group's row overwrites the last pivot's
+      const int grp = threadIdx.x / g.nl, lane = threadIdx.x - grp * g.nl;
+      if (grp < ngrp && lane * V < npitch) {
+        typename SqT<T>::type sq{};
+        for (int i = grp; i < g.m; i += ngrp)
+          sq = v_sq(*reinterpret_cast<const VT*>(tab + (size_t)i * g.ldw + lane * V), sq);
+        store_partials(npart + (size_t)grp * npitch + lane * V, sq);
+      }
+      __syncthreads();
+      return;
+    }
     for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = make_uint2(0u, 0u);
     __syncthreads();
     const int nt = (int)blockDim.x, G = min(nt / g.nl, kMaxNormGroups);
@@ -938,7 +983,7 @@ struct Solver {
         if (bland) {
           kk = price_key(v, j, c0 + lj, true);
         } else {
-          const float gm = norm_gamma(gam[lj]);
+          const float gm = npart ? part_gamma(lj) : norm_gamma(gam[lj]);
           const float vf = (float)v;
           float sc = __fdividef(vf * vf, gm);
           if (w) sc *= w[j];
@@ -986,7 +1031,8 @@ struct Solver {
         // the norms are summed afresh by this pivot's sweep (the pricing
         // reads are done: its argmin ended with a barrier); the column is
         // extracted inside the ratio test's first pass (FP32: and cleared)
-        for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = make_uint2(0u, 0u);
+        if (!npart)
+          for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = make_uint2(0u, 0u);
         kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta, s, kPre, kRecip);
       } else {
         const int owner = s / g.cw;
@@ -2463,6 +2509,16 @@ struct Solver {
         continue;
       }
       place(L, m);
+      // FP32 on one CTA: the norms as partial sums where they fit the region
+      npart = nullptr;
+      if (kFP32 && !CLUSTER && gam) {
+        const int G = min(nt / g.nl, kMaxNormGroups);
+        if ((size_t)G * g.cw * 4 <= (size_t)L.gbytes) {
+          npart = reinterpret_cast<float*>(gam);
+          npitch = g.cw;
+          ngrp = G;
+        }
+      }
       const int c0 = rank * g.cw;
       const int lc = max(0, min(g.cw, g.Wc - c0));
       load(g, c0, lc, A, b, c, A32, a, lp);
