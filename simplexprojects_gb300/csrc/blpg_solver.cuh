@@ -523,8 +523,8 @@ struct Solver {
   int* cvar;   // slot -> variable id (every slot of the LP, replicated per CTA)
   int* vpos;   // variable -> slot if nonbasic, -1 - row if basic
   uint2* gam;  // steepest edge: fixed-point column norms of the local slots
-  float* npart;  // or their per-row-group partial sums (null: the counters)
-  int npitch, ngrp;  // partial sums: row pitch (cw) and row groups
+  int ngrp;     // or, when > 0, that many rows of per-row-group partial sums
+                // of slots [0, cw) in the same region (row pitch cw)
   double* xr;  // FP64 x_B of the refresh (FP32 tableaux, FP64 ones with steepest edge)
   double* yr;  // FP64 duals of the refresh
   float* rf;   // the refresh's residuals rounded to FP32 / a 32-bit list
@@ -752,7 +752,7 @@ struct Solver {
   // The RHS replica is not extracted: the next ratio test reads the tableau.
   __device__ void update_body_se32(const Geom& g, int r, const T* fcol, int lc) {
     update_rows<true, true>(tab, rhsx, rank, g.m, g.ldw, g.nl, g.cw, r, -1, fcol, -1, -1, 0,
-                            nullptr, gam, lc, npart);
+                            nullptr, gam, lc, ngrp ? reinterpret_cast<float*>(gam) : nullptr);
   }
   // Kept out of line with plain arguments (no `this`, no structs by
   // reference) so that the unrolled sweep has its own register budget and
@@ -930,22 +930,30 @@ struct Solver {
   static __device__ __forceinline__ void store_partials(float* dst, const float2& sq) {
     *reinterpret_cast<float2*>(dst) = make_float2(norm_clamp(sq.x), norm_clamp(sq.y));
   }
-  // gamma_j of local slot lj from the partial sums, added in row-group order.
-  __device__ __forceinline__ float part_gamma(int lj) const {
+  // gamma_j of local slot lj from the partial sums, added in row-group order
+  // (the first eight loaded together; the zeros past ngrp add exactly, the
+  // partials being >= 0).
+  __device__ __forceinline__ float part_gamma(int lj, int cw) const {
+    const float* p = reinterpret_cast<const float*>(gam) + lj;
+    float v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = q < ngrp ? p[q * cw] : 0.f;
     float acc = 0.f;
-    for (int q = 0; q < ngrp; ++q) acc += npart[q * npitch + lj];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc += v[q];
+    for (int q = 8; q < ngrp; ++q) acc += p[q * cw];
     return 1.f + acc;
   }
   __device__ void norms_full(const Geom& g, int lc) {
-    if (npart) {
+    if (ngrp) {
       // the partial sums of every row group, grouped as the sweep groups
       // them; each group's row overwrites the last pivot's
       const int grp = threadIdx.x / g.nl, lane = threadIdx.x - grp * g.nl;
-      if (grp < ngrp && lane * V < npitch) {
+      if (grp < ngrp && lane * V < g.cw) {
         typename SqT<T>::type sq{};
         for (int i = grp; i < g.m; i += ngrp)
           sq = v_sq(*reinterpret_cast<const VT*>(tab + (size_t)i * g.ldw + lane * V), sq);
-        store_partials(npart + (size_t)grp * npitch + lane * V, sq);
+        store_partials(reinterpret_cast<float*>(gam) + (size_t)grp * g.cw + lane * V, sq);
       }
       __syncthreads();
       return;
@@ -983,7 +991,7 @@ struct Solver {
         if (bland) {
           kk = price_key(v, j, c0 + lj, true);
         } else {
-          const float gm = npart ? part_gamma(lj) : norm_gamma(gam[lj]);
+          const float gm = ngrp ? part_gamma(lj, g.cw) : norm_gamma(gam[lj]);
           const float vf = (float)v;
           float sc = __fdividef(vf * vf, gm);
           if (w) sc *= w[j];
@@ -1031,7 +1039,7 @@ struct Solver {
         // the norms are summed afresh by this pivot's sweep (the pricing
         // reads are done: its argmin ended with a barrier); the column is
         // extracted inside the ratio test's first pass (FP32: and cleared)
-        if (!npart)
+        if (!ngrp)
           for (int lj = threadIdx.x; lj < g.ldw; lj += blockDim.x) gam[lj] = make_uint2(0u, 0u);
         kr = ratio(g, colbuf(cur), piv_tol, feas_tol, a.harris && !bland, theta, s, kPre, kRecip);
       } else {
@@ -2510,14 +2518,10 @@ struct Solver {
       }
       place(L, m);
       // FP32 on one CTA: the norms as partial sums where they fit the region
-      npart = nullptr;
+      ngrp = 0;
       if (kFP32 && !CLUSTER && gam) {
         const int G = min(nt / g.nl, kMaxNormGroups);
-        if ((size_t)G * g.cw * 4 <= (size_t)L.gbytes) {
-          npart = reinterpret_cast<float*>(gam);
-          npitch = g.cw;
-          ngrp = G;
-        }
+        if ((size_t)G * g.cw * 4 <= (size_t)L.gbytes) ngrp = G;
       }
       const int c0 = rank * g.cw;
       const int lc = max(0, min(g.cw, g.Wc - c0));
