@@ -255,6 +255,28 @@ __device__ __forceinline__ Key block_min(const Key& k, Key* red) {
   return warp_min<W1>(v);
 }
 
+// Block-wide minimum of the value words only (w0, and w1 with W1): every
+// thread returns them, w2 = w3 = 0, or key_none() when no thread had a
+// value.  For a minimum whose ties do not matter (Harris's first pass).  One
+// __syncthreads, `red` as block_min.
+template <bool W1 = true>
+__device__ __forceinline__ Key block_min_value(const Key& k, Key* red) {
+  const unsigned full = 0xffffffffu;
+  auto vmin = [&](unsigned a0, unsigned a1, unsigned& r0, unsigned& r1) {
+    r0 = __reduce_min_sync(full, a0);
+    r1 = W1 ? __reduce_min_sync(full, a0 == r0 ? a1 : ~0u) : 0u;
+  };
+  unsigned w0, w1;
+  vmin(k.w0, k.w1, w0, w1);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) red[warp] = Key{w0, w1, 0u, 0u};
+  __syncthreads();
+  const int nw = (int)(blockDim.x >> 5);
+  const Key v = lane < nw ? red[lane] : key_none();
+  vmin(v.w0, v.w1, w0, w1);
+  return w0 == ~0u ? key_none() : Key{w0, w1, 0u, 0u};
+}
+
 // Pricing key of reduced cost d of variable j in column slot s (only
 // d < -tol is eligible).  For negative numbers ~bits is increasing in the
 // value, so the most negative d has the smallest key; ties go to the lowest
@@ -662,7 +684,8 @@ struct Solver {
         if (key_less(kk, k)) k = kk;
       }
     }
-    k = block_min<kW1>(k, redR);
+    // only the bound matters here, not which row gives it
+    k = block_min_value<kW1>(k, redR);
     if (k.w2 == ~0u) return k;
     const T tmax = key_theta(k, T(0));
     Key k2 = key_none();
