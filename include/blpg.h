@@ -402,9 +402,11 @@ int32_t blpg_topm_hint(const float* d_scores, int32_t lds, int32_t count,
  * precision and tolerances are kept, pricing is set to steepest edge) and
  * the device buffers.  blpg_learned_solve then takes HOST arrays of that
  * batch (same shapes and offsets) and the family id of each LP, uploads
- * them, runs features -> network -> weights -> solve on one stream and
- * downloads status, objective and (when non-null) x, pivots and info;
- * synchronous.  Pinned host arrays upload fastest. */
+ * them, runs features -> network -> weights -> solve and downloads status,
+ * objective and (when non-null) x, pivots and info; synchronous.  From 512
+ * LPs on, b, c and the family ids upload in two halves and each half's
+ * features and network run as soon as it has landed, while the rest (then
+ * A) uploads.  Pinned host arrays upload fastest. */
 typedef struct blpg_learned blpg_learned;
 int32_t blpg_learned_create(blpg_mlp* mlp, int32_t families, const float* host_mean,
                             const float* host_std, float beta, const blpg_batch* shapes,
