@@ -197,13 +197,11 @@ extern "C" int32_t blpg_learned_create(blpg_mlp* mlp, int32_t families, const fl
   return BLPG_OK;
 }
 
-extern "C" int32_t blpg_learned_solve(blpg_learned* L, const blpg_batch* bt,
-                                      const int32_t* host_family, blpg_result* out) {
-  using blpg::fail;
-  if (!L || !bt || !host_family || !out || !out->status || !out->objective)
-    return fail(BLPG_EINVAL, "blpg_learned_solve: null argument");
-  if (bt->count != L->count || !bt->A || !bt->b || !bt->c)
-    return fail(BLPG_EINVAL, "blpg_learned_solve: the batch is not the one the solver was made for");
+namespace {
+
+// The body of blpg_learned_solve, arguments checked.
+int32_t learned_solve(blpg_learned* L, const blpg_batch* bt, const int32_t* host_family,
+                      blpg_result* out) {
   const int N = L->count, H = L->half;
   cudaStream_t s = L->stream, u = L->stream_a;
   const size_t d8 = sizeof(double);
@@ -263,6 +261,25 @@ extern "C" int32_t blpg_learned_solve(blpg_learned* L, const blpg_batch* bt,
   if (out->pivots) std::memcpy(out->pivots, h + 12 * (size_t)N, sizeof(int32_t) * N);
   if (out->info) std::memcpy(out->info, h + 16 * (size_t)N, sizeof(int32_t) * N);
   return BLPG_OK;
+}
+
+}  // namespace
+
+extern "C" int32_t blpg_learned_solve(blpg_learned* L, const blpg_batch* bt,
+                                      const int32_t* host_family, blpg_result* out) {
+  using blpg::fail;
+  if (!L || !bt || !host_family || !out || !out->status || !out->objective)
+    return fail(BLPG_EINVAL, "blpg_learned_solve: null argument");
+  if (bt->count != L->count || !bt->A || !bt->b || !bt->c)
+    return fail(BLPG_EINVAL, "blpg_learned_solve: the batch is not the one the solver was made for");
+  const int32_t rc = learned_solve(L, bt, host_family, out);
+  if (rc != BLPG_OK) {
+    // a step failed with copies or kernels of this call still queued: let
+    // them finish before the next call overwrites their buffers
+    cudaStreamSynchronize(L->stream_a);
+    cudaStreamSynchronize(L->stream);
+  }
+  return rc;
 }
 
 extern "C" void blpg_learned_destroy(blpg_learned* L) {
