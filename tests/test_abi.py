@@ -79,3 +79,21 @@ def test_batch_view_copies_are_independent(built):
     assert C.addressof(again.c.contents) == b.c.ctypes.data
     b.c = b.c.copy()
     assert C.addressof(b.c_struct().c.contents) == b.c.ctypes.data
+
+
+def test_batch_offsets_packed_and_given(built):
+    """LPBatch.offsets(): offsets a batch carries come back as they are;
+    missing ones are the packed layout (each LP right after the previous)."""
+    b = sp.generate(1, 30, seed=5)
+    oA, ob, oc = b.offsets()
+    m, n = b.m.astype(np.int64), b.n.astype(np.int64)
+    assert np.array_equal(oA, np.concatenate([[0], np.cumsum(m * n)[:-1]]))
+    assert np.array_equal(ob, np.concatenate([[0], np.cumsum(m)[:-1]]))
+    assert np.array_equal(oc, np.concatenate([[0], np.cumsum(n)[:-1]]))
+    assert oA.dtype == ob.dtype == oc.dtype == np.int64
+    shared = sp.generate(4, 40, seed=6, share_family_A=True)
+    sA, sb, sc = shared.offsets()
+    assert sA is shared.off_A
+    e = np.empty(0)
+    empty = sp.LPBatch(np.empty(0, np.int32), np.empty(0, np.int32), e, e, e)
+    assert all(o.size == 0 for o in empty.offsets())
