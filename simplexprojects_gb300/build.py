@@ -50,6 +50,7 @@ def _nvcc() -> str:
 # (source, extra nvcc flags)
 SOURCES = [
     ("blpg_api.cu", ["--fmad=false"]),
+    ("blpg_part.cu", ["--fmad=false"]),
     ("blpg_peaks.cu", []),
     ("blpg_noalloc.cu", ["--fmad=false"]),
     ("blpg_mlp.cu", []),

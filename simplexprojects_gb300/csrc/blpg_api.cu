@@ -30,6 +30,14 @@
 #include "blpg_solver.cuh"
 
 namespace blpg {
+// solve_kernel<float, false, true> (partial-sum norm layouts), in blpg_part.cu
+cudaError_t part_set_attrs(int max_smem);
+cudaError_t part_occupancy(int* ctas_per_sm, int nt, int smem);
+cudaError_t part_launch(int grid, int nt, int smem, cudaStream_t s, const dev::LpArgs& a,
+                        const dev::ClassArgs& ca);
+}  // namespace blpg
+
+namespace blpg {
 
 static thread_local std::string g_err;
 
@@ -98,6 +106,7 @@ struct ClassPlan {
   int max_ns = 0;  // most structural basics any member can have: min(m, n)
   long long lu_off = 0, lu_stride = 0;  // the class's LU refresh scratch (doubles)
   int ctas_per_sm = 1;
+  int part = 0;  // FP32 steepest edge on one CTA: launched with the partial-sum norm layout
   int count = 0, grid = 0, order_off = 0;
   double work = 0;
 };
@@ -186,9 +195,13 @@ static int occupancy(const ClassPlan& c, int* ctas_per_sm, int* clusters) {
   *ctas_per_sm = 0;
   *clusters = 0;
   if (c.K == 1) {
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm,
-                                                     dev::solve_kernel<T, false>, c.nt,
-                                                     c.smem));
+    if (sizeof(T) == 4 && c.part) {
+      CK(part_occupancy(ctas_per_sm, c.nt, c.smem));
+    } else {
+      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm,
+                                                       dev::solve_kernel<T, false>, c.nt,
+                                                       c.smem));
+    }
   } else {
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[1];
@@ -350,6 +363,26 @@ static int build_classes(blpg_plan* p, int max_smem, int max_cluster) {
     int per_sm = 0, clusters = 0;
     int rc = occupancy<T>(c, &per_sm, &clusters);
     if (rc) return rc;
+    // FP32 steepest edge on one CTA: when some member's norm partial sums (a
+    // row per row group of this class's thread count) do not fit the region
+    // its layout has, the class takes the kernel whose layouts grow that
+    // region, if that costs no residency
+    if (elem == 4 && se && c.K == 1) {
+      ClassPlan cp = c;
+      cp.part = 1;
+      for (int lp : lps) {
+        const int m = p->m[lp], n = p->n[lp], na = p->na[lp];
+        const Geom g(m, n, na, 1, V);
+        const int pb = std::min(c.nt / g.nl, dev::kMaxNormGroups) * g.cw * 4;
+        cp.smem = std::max(cp.smem, Layout(m, g.ldw, n + m + na, elem, se, pb).total);
+      }
+      int per_sm2 = 0, clusters2 = 0;
+      if (cp.smem > c.smem && cp.smem <= max_smem &&
+          occupancy<T>(cp, &per_sm2, &clusters2) == BLPG_OK && per_sm2 >= per_sm) {
+        c.smem = cp.smem;
+        c.part = 1;
+      }
+    }
     const int slots = c.K == 1 ? per_sm * p->sm_count : clusters;
     if (slots <= 0)
       return fail(BLPG_ETOOBIG, "class K=%d nt=%d smem=%d cannot be resident", c.K, c.nt,
@@ -386,7 +419,11 @@ static int launch_one(blpg_plan* p, size_t ci, const LpArgs& args, cudaStream_t 
   ca.lu = p->d_lu ? p->d_lu + c.lu_off : nullptr;
   ca.lu_stride = c.lu_stride;
   if (c.K == 1) {
-    dev::solve_kernel<T, false><<<c.grid, c.nt, c.smem, s>>>(args, ca);
+    if (sizeof(T) == 4 && c.part) {
+      CK(part_launch(c.grid, c.nt, c.smem, s, args, ca));
+    } else {
+      dev::solve_kernel<T, false><<<c.grid, c.nt, c.smem, s>>>(args, ca);
+    }
     CK(cudaGetLastError());
   } else {
     cudaLaunchConfig_t cfg = {};
@@ -702,6 +739,11 @@ extern "C" int32_t blpg_plan_create(const blpg_batch* bt, const blpg_options* op
   const int max_smem = (int)prop.sharedMemPerBlockOptin;
   if (p->precision == BLPG_FP32) {
     if ((rc = set_kernel_attrs<float, false>(max_smem))) return rc;
+    {
+      const cudaError_t e = part_set_attrs(max_smem);
+      if (e != cudaSuccess)
+        return fail(BLPG_ECUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+    }
     if ((rc = set_kernel_attrs<float, true>(max_smem))) return rc;
     if ((rc = set_kernel_attrs<double, false>(max_smem))) return rc;  // the FP64 pass
     if ((rc = set_kernel_attrs<double, true>(max_smem))) return rc;

@@ -161,7 +161,9 @@ struct Geom {
 // only needs the largest member's total.
 struct Layout {
   int tab, colA, colB, rhsx, basis, flags, cvar, vpos, ext, red, state, gam, gbytes, total;
-  __host__ __device__ Layout(int m, int ldw, int nv, int elem, int se = 0) {
+  // pbytes: bytes the norm region must hold for partial sums (0: the counters
+  // and whatever the region has anyway)
+  __host__ __device__ Layout(int m, int ldw, int nv, int elem, int se = 0, int pbytes = 0) {
     const int mp1 = round_up(m + 1, 4);
     const int nvp = round_up(nv, 4);
     state = 0;
@@ -196,12 +198,17 @@ struct Layout {
     gbytes = 0;
     if (se) {
       if (ext_bytes >= ldw * 8) {
+        // over the refresh's region, extended past it for partial sums
         gam = ext;
         gbytes = ext_bytes;
+        if (pbytes > gbytes) {
+          off += round_up(pbytes - gbytes, 16);
+          gbytes += round_up(pbytes - gbytes, 16);
+        }
       } else {
         off = round_up(off, 16);
         gam = off;
-        gbytes = round_up(ldw * 8, 16);
+        gbytes = round_up(ldw * 8 > pbytes ? ldw * 8 : pbytes, 16);
         off += gbytes;
       }
     }
@@ -2501,6 +2508,9 @@ struct Solver {
     gam = L.gam >= 0 ? reinterpret_cast<uint2*>(smem + L.gam) : nullptr;
   }
 
+  // PART: the class's layouts hold the FP32 steepest-edge norms as partial
+  // sums of this CTA's row groups (the norm region grown to fit them)
+  template <bool PART>
   __device__ void run(const LpArgs& a, const ClassArgs& ca) {
     const int tid = threadIdx.x, nt = blockDim.x;
     constexpr bool kFP32 = sizeof(T) == 4;
@@ -2526,7 +2536,8 @@ struct Solver {
       for (int i = tid; i < m; i += nt) na += b[i] < 0.0 ? 1 : 0;
       na = block_sum(na);
       const Geom g(m, n, na, K, V);
-      const Layout L(m, g.ldw, n + m + na, (int)sizeof(T), ca.se);
+      const int pbytes = PART ? min(nt / g.nl, kMaxNormGroups) * g.cw * 4 : 0;
+      const Layout L(m, g.ldw, n + m + na, (int)sizeof(T), ca.se, pbytes);
       if (L.total > ca.smem || na > ca.max_na || g.nl > (int)blockDim.x) {
         // the LP does not fit the layout this plan was built for (e.g. a
         // plan made without b has no room for phase-I columns): refuse it
@@ -2732,7 +2743,7 @@ struct Solver {
   }
 };
 
-template <typename T, bool CLUSTER>
+template <typename T, bool CLUSTER, bool PART = false>
 __global__ void __launch_bounds__(512, 1) solve_kernel(const __grid_constant__ LpArgs a,
                                                         const __grid_constant__ ClassArgs ca) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -2746,7 +2757,7 @@ __global__ void __launch_bounds__(512, 1) solve_kernel(const __grid_constant__ L
   s.K = ca.K;
   s.rank = CLUSTER ? (int)cg::this_cluster().block_rank() : 0;
   s.lu = ca.lu ? ca.lu + (size_t)(blockIdx.x / ca.K) * (size_t)ca.lu_stride : nullptr;
-  s.run(a, ca);
+  s.template run<PART>(a, ca);
 }
 
 }  // namespace dev
