@@ -147,3 +147,26 @@ def test_cli_batch_mode_matches_the_library(built, tmp_path, bits):
     else:
         ok = want.status == 5
         assert np.allclose(ob[ok], want.objective[ok], rtol=1e-9, atol=1e-9)
+
+
+def test_unsupported_version_and_bad_header(built, tmp_path):
+    batch = sp.generate(1, 3, seed=36)
+    path = tmp_path / "ok.blpg"
+    sp.write_batch(path, batch)
+    raw = bytearray(path.read_bytes())
+    bad = tmp_path / "bad.blpg"
+    v2 = bytearray(raw)
+    v2[8:12] = np.uint32(2).tobytes()               # version 2
+    bad.write_bytes(bytes(v2))
+    with pytest.raises(sp.BlpgError) as e:
+        sp.read_batch(bad)
+    assert e.value.code == -6 and "version" in str(e.value)
+    neg = bytearray(raw)
+    neg[16:24] = np.int64(-1).tobytes()             # count
+    bad.write_bytes(bytes(neg))
+    with pytest.raises(sp.BlpgError) as e:
+        sp.read_batch(bad)
+    assert e.value.code == -6 and "header" in str(e.value)
+    bad.write_bytes(bytes(raw[:20]))                # cut inside the sizes
+    with pytest.raises(sp.BlpgError):
+        sp.read_batch(bad)
