@@ -407,6 +407,20 @@ extern "C" int32_t blpg_read_batch(const char* path, int64_t* count, int64_t* nA
   if (std::fread(sizes, 8, 4, f) != 4 || sizes[0] < 0 || sizes[0] > INT32_MAX || sizes[1] < 0 ||
       sizes[2] < 0 || sizes[3] < 0)
     return fail(BLPG_EIO, "blpg_read_batch: %s: bad header", path);
+  // the file must be exactly as long as its header says, so that a damaged
+  // header cannot make a caller allocate for data that is not there
+  {
+    const uint64_t cnt = (uint64_t)sizes[0], big = (uint64_t)1 << 58;  // 8 x 3 x 2^58 < 2^63
+    bool fits = (uint64_t)sizes[1] < big && (uint64_t)sizes[2] < big && (uint64_t)sizes[3] < big;
+    const uint64_t want = 48 + cnt * 32 + 8 * ((uint64_t)sizes[1] + (uint64_t)sizes[2] +
+                                              (uint64_t)sizes[3]);
+    long here = std::ftell(f), end = -1;
+    if (here >= 0 && std::fseek(f, 0, SEEK_END) == 0) end = std::ftell(f);
+    if (end < 0 || std::fseek(f, here, SEEK_SET) != 0)
+      return fail(BLPG_EIO, "blpg_read_batch: %s: cannot seek", path);
+    if (!fits || (uint64_t)end != want)
+      return fail(BLPG_EIO, "blpg_read_batch: %s is truncated or its header is damaged", path);
+  }
   *count = sizes[0];
   *nA = sizes[1];
   *nb = sizes[2];

@@ -170,3 +170,24 @@ def test_unsupported_version_and_bad_header(built, tmp_path):
     bad.write_bytes(bytes(raw[:20]))                # cut inside the sizes
     with pytest.raises(sp.BlpgError):
         sp.read_batch(bad)
+
+
+def test_header_claiming_more_data_than_the_file_holds(built, tmp_path):
+    """A damaged size in the header is refused before any buffer is sized
+    from it (the first call of the two already fails)."""
+    batch = sp.generate(1, 4, seed=37)
+    path = tmp_path / "ok.blpg"
+    sp.write_batch(path, batch)
+    raw = bytearray(path.read_bytes())
+    for field, value in ((24, 10**15), (32, 2**62), (40, 3)):   # nA, nb, nc
+        bad = bytearray(raw)
+        bad[field:field + 8] = np.int64(value).tobytes()
+        p = tmp_path / f"bad{field}.blpg"
+        p.write_bytes(bytes(bad))
+        with pytest.raises(sp.BlpgError) as e:
+            sp.read_batch(p)
+        assert e.value.code == -6 and ("damaged" in str(e.value) or "header" in str(e.value))
+    longer = tmp_path / "longer.blpg"
+    longer.write_bytes(bytes(raw) + b"\0" * 8)      # trailing bytes: not this batch's file
+    with pytest.raises(sp.BlpgError):
+        sp.read_batch(longer)
